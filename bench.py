@@ -1,0 +1,368 @@
+"""Benchmark of the WHIR prover path on GB300.
+
+Workload (the reference's headline configuration on one GPU): WHIR PCS commit + prove, d = 24
+(2^24 uniform random Goldilocks coefficients, codeword 2^25 elements), Basefield<Field64_2>
+(Goldilocks2), Blake3 Merkle trees, log_inv_rate 1, folding factor 4, security 100, unique decoding,
+pow_bits 20, one uniform random evaluation point. Inputs are seeded synthetic data (SplitMix64,
+whir_gb300/inputs.py). The metric is milliseconds per proof (commit + prove, as the reference's
+benchmark.rs:238-258 times it); lower is better.
+
+One step = one full proof. `value` times steps with the polynomial already resident in HBM;
+`e2e` times the same proofs through the public C ABI from pinned host memory (the host->device
+copy of the coefficients and every device->host read of the proof happen inside the timed region).
+Every proof's working set (>1 GiB) exceeds L2 (129 MB), and an L2-sized buffer is also rewritten
+between steps.
+
+--impl reference runs the reference's CPU algorithm (the repository's C++ restatement in oracle/,
+since the Rust reference cannot be built here) on all host cores for the same workload.
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+# DRAM bytes per launch of the dominant kernel from an ncu capture (profiles/ summaries), keyed by
+# family; None until captured.
+NCU_TRAFFIC_PER_CALL = {}
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nv", type=int, default=24)
+    ap.add_argument("--cpu-nv", type=int, default=20, help="size of the bounded CPU-baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend="gloo")
+    return rank, world, local, dist
+
+
+def max_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload(nv):
+    import whir_gb300 as W
+    from whir_gb300.inputs import Rng, field_elements
+    params = W.ProtocolParameters(unique_decoding=True, security_level=100, pow_bits=20, starting_log_inv_rate=1,
+                                  initial_folding_factor=4, folding_factor=4, hash_id="Blake3")
+    rng = Rng(2)  # seed = config index
+    vec = rng.goldilocks(1 << nv)
+    point = field_elements("Goldilocks2", nv, rng=rng).reshape(nv, 2)
+    return params, vec, point
+
+
+def evaluation(vec, point):
+    import oracle
+    return oracle.multilinear_extend(oracle.GOLDILOCKS2, vec, point.reshape(-1))
+
+
+def algorithmic_bytes(cfg_json, nv):
+    """Per-proof algorithmic HBM bytes of each kernel family (input + output of each pass)."""
+    s_elem, t_elem = 8, 16
+    enc = 0
+    ic = cfg_json["initial_committer"]
+    enc += ic["vector_size"] * ic["num_vectors"] * s_elem + ic["codeword_length"] * ic["num_cols"] * s_elem
+    for r in cfg_json["rounds"]:
+        c = r["irs"]
+        enc += c["vector_size"] * t_elem + c["codeword_length"] * c["num_cols"] * t_elem
+    sc = 0
+    sizes = [(cfg_json["initial_sumcheck"]["initial_size"], cfg_json["initial_sumcheck"]["num_rounds"])]
+    sizes += [(r["sumcheck"]["initial_size"], r["sumcheck"]["num_rounds"]) for r in cfg_json["rounds"]]
+    for n, rounds in sizes:
+        for k in range(rounds):
+            m = n >> k
+            sc += 2 * m * t_elem + (m * t_elem if k > 0 else 0)  # read a, b (+ write halves when folding)
+        sc += 2 * (n >> rounds) * t_elem * 2  # final fold of a and b
+    lift = (1 << nv) * (s_elem + t_elem)
+    eq = (1 << nv) * t_elem * 2  # read-modify-write of the covector
+    return {"encode": enc, "sumcheck": sc, "lift": lift, "eq": eq}
+
+
+def hbm_peak():
+    try:
+        d = json.load(open(MEASURED_PEAKS))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def cpu_baseline(args, params, vec_full, point_full):
+    """Times the oracle prover (the reference algorithm restated in C++) on a bounded sample."""
+    import oracle
+    from whir_gb300.inputs import Rng, field_elements
+    nv = args.cpu_nv
+    rng = Rng(2)
+    vec = rng.goldilocks(1 << nv)
+    point = field_elements("Goldilocks2", nv, rng=rng).reshape(nv, 2)
+    ev = oracle.multilinear_extend(oracle.GOLDILOCKS2, vec, point.reshape(-1))
+    op = oracle.make_params(unique_decoding=True, security_level=100, pow_bits=20)
+    t0 = time.perf_counter()
+    runs = 0
+    while True:
+        oracle.whir_prove(oracle.GOLDILOCKS2, op, nv, "bench", vec.reshape(1, -1), [point], [], [[ev]])
+        runs += 1
+        if time.perf_counter() - t0 > 10.0 or runs >= 3:
+            break
+    sec = (time.perf_counter() - t0) / runs
+    scale = 1 << (args.nv - nv)
+    return {"value": sec * 1e3 * scale, "unit": "ms", "cores": oracle.lib().oracle_num_threads(), "kind": "port",
+            "sample": "%d proof(s) at d=%d (%.2f s each), scaled x%d (linear in size) to d=%d"
+                      % (runs, nv, sec, scale, args.nv)}
+
+
+def run_reference(args):
+    rank, world, local, dist = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    import oracle
+    nv = args.cpu_nv
+    from whir_gb300.inputs import Rng, field_elements
+    rng = Rng(2)
+    vec = rng.goldilocks(1 << nv)
+    point = field_elements("Goldilocks2", nv, rng=rng).reshape(nv, 2)
+    ev = oracle.multilinear_extend(oracle.GOLDILOCKS2, vec, point.reshape(-1))
+    op = oracle.make_params(unique_decoding=True, security_level=100, pow_bits=20)
+    for _ in range(args.warmup):
+        oracle.whir_prove(oracle.GOLDILOCKS2, op, nv, "bench", vec.reshape(1, -1), [point], [], [[ev]])
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.whir_prove(oracle.GOLDILOCKS2, op, nv, "bench", vec.reshape(1, -1), [point], [], [[ev]])
+    sec = (time.perf_counter() - t0) / args.steps
+    scale = 1 << (args.nv - nv)
+    ms = sec * 1e3 * scale
+    cores = oracle.lib().oracle_num_threads()
+    line = {
+        "impl": "reference", "metric": "prove_ms_d%d_goldilocks2_blake3" % args.nv, "value": ms, "unit": "ms",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks field)",
+        "data": "synthetic (SplitMix64 seed 2)",
+        "config": {"workload": "WHIR PCS commit+prove d=%d Goldilocks2 Blake3 rate 1/2 k=4 sec 100 UD pow 20, 1 point"
+                               % args.nv},
+        "cpu_baseline": {"value": ms, "unit": "ms", "cores": cores, "kind": "port",
+                         "sample": "each step: 1 proof at d=%d scaled x%d to d=%d" % (nv, scale, args.nv)},
+        "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import torch
+
+    import whir_gb300 as W
+    rank, world, local, dist = dist_setup(args.gpus)
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    nv = args.nv
+    params, vec, point = workload(nv)
+    ev = evaluation(vec, point)
+    ctx = W.Context(dev)
+    cfg = W.Config("Goldilocks2", 1 << nv, params)
+    cfg_json = cfg.json()
+    stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda:%d" % dev)
+
+    # Resident input for `value`.
+    d_vec = ctx.alloc(vec.nbytes)
+    ctx.upload(d_vec, vec)
+
+    def one_proof(on_device, src):
+        ps = W.ProverState(cfg, "bench")
+        w = cfg.commit(ctx, ps, src, on_device=on_device)
+        cfg.prove(ctx, ps, src, [w], [point], [], [[ev]], on_device=on_device)
+        w.free()
+        return ps
+
+    ref_narg = None
+    for _ in range(args.warmup):
+        ps = one_proof(True, d_vec)
+        ref_narg = ps.proof()
+    barrier(dist)
+    torch.cuda.synchronize()
+
+    times = []
+    launches0 = ctx.launch_count()
+    ctx.set_profiling(True)
+    sampler = ClockSampler(dev)
+    sampler.start()
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ps = one_proof(True, d_vec)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+        assert ps.proof() == ref_narg, "proof bytes changed between runs"
+    clocks = sampler.stop()
+    prof = ctx.profile()
+    ctx.set_profiling(False)
+    launches = ctx.launch_count() - launches0
+    barrier(dist)
+    torch.cuda.synchronize()
+    total_ms = max_over_ranks(dist, float(np.sum(times)))
+    ms_per_proof_job = total_ms / (args.steps * world)
+
+    # End to end through the public API from pinned host memory.
+    e2e = None
+    if not args.no_e2e:
+        pinned = torch.empty(vec.size, dtype=torch.int64).pin_memory()
+        host = pinned.numpy().view(np.uint64)
+        host[:] = vec
+        for _ in range(max(1, args.warmup // 2)):
+            one_proof(False, host)
+        h0, d0 = ctx.transfer_bytes()
+        et = []
+        for _ in range(args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ps = one_proof(False, host)
+            e1.record(stream)
+            e1.synchronize()
+            et.append(e0.elapsed_time(e1))
+        h1, d1 = ctx.transfer_bytes()
+        e2e_total = max_over_ranks(dist, float(np.sum(et)))
+        e2e = {"value": e2e_total / (args.steps * world), "unit": "ms",
+               "h2d_bytes_per_step": int((h1 - h0) / args.steps), "d2h_bytes_per_step": int((d1 - d0) / args.steps)}
+
+    if rank != 0:
+        return
+    # Roofline of the dominant kernel family, timed live with CUDA events on the context's stream.
+    alg = algorithmic_bytes(cfg_json, nv)
+    fam = max((f for f in prof if prof[f][1] > 0), key=lambda f: prof[f][0])
+    ms_f, calls_f = prof[fam]
+    peak, peak_kind = hbm_peak()
+    roofline = None
+    if fam in alg:
+        per_call_bytes = alg[fam] * args.steps / calls_f
+        achieved = per_call_bytes / (ms_f / calls_f * 1e-3) / 1e9
+        roofline = {"bound": "hbm", "kernel_family": fam, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "peak_source": peak_kind,
+                    "traffic": NCU_TRAFFIC_PER_CALL.get(fam), "algorithmic_bytes_per_launch": per_call_bytes,
+                    "avg_launch_ms": ms_f / calls_f}
+    else:
+        roofline = {"bound": "integer", "kernel_family": fam, "achieved": None, "peak": peak, "unit": "GB/s",
+                    "frac": None, "traffic": NCU_TRAFFIC_PER_CALL.get(fam), "avg_launch_ms": ms_f / calls_f}
+    cpu = None if args.no_cpu_baseline else cpu_baseline(args, params, vec, point)
+    line = {
+        "metric": "prove_ms_d%d_goldilocks2_blake3" % nv, "value": ms_per_proof_job, "unit": "ms",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(times)),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks field)",
+        "data": "synthetic (SplitMix64 seed 2, uniform field elements)",
+        "config": {"workload": "WHIR PCS commit+prove d=%d Goldilocks2 Blake3 rate 1/2 k=4 sec 100 UD pow 20, 1 point"
+                               % nv, "parallelism": "replicas x%d" % world,
+                   "l2": "working set > L2 and a 256 MiB buffer rewritten between steps",
+                   "p50_ms": float(np.percentile(times, 50)), "p99_ms": float(np.percentile(times, 99))},
+        "roofline": roofline,
+        "kernel_families_ms_per_proof": {k: v[0] / args.steps for k, v in prof.items() if v[1]},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

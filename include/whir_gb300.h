@@ -1,0 +1,173 @@
+/* whir_gb300 — C ABI of the GB300 (sm_103a) WHIR prover path.
+ *
+ * Each entry point replaces one interface of the reference crate (WizardOfMenlo/whir); the
+ * citation beside it names the Rust item it stands in for. Conventions:
+ *   - Every function returns 0 on success or a negative whir_status; none aborts the process.
+ *     whir_last_error() describes the last failure on the calling thread.
+ *   - Field elements are canonical little-endian u64 limbs (Goldilocks: 1 limb per base
+ *     coefficient); extension elements list their base coefficients in increasing degree.
+ *   - Pointers are host pointers unless a `flags` argument carries WHIR_DEVICE_PTRS, in which case
+ *     the data pointers are device pointers on the context's device.
+ *   - A whir_ctx owns one CUDA stream and a stream-ordered memory pool; calls on one context must
+ *     not overlap (serialise them per context); different contexts may be used from different
+ *     threads.
+ *   - There is no CPU fallback: without a usable CUDA device whir_ctx_create fails with
+ *     WHIR_ERR_NO_DEVICE.
+ */
+#ifndef WHIR_GB300_H
+#define WHIR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum whir_status {
+  WHIR_OK = 0,
+  WHIR_REJECT = 1,           /* verifier rejected (VerificationError) */
+  WHIR_ERR_INVALID = -1,     /* bad argument: size mismatch, unknown id, non-canonical element */
+  WHIR_ERR_UNSUPPORTED = -2, /* shape valid for the reference but not implemented on the device */
+  WHIR_ERR_CUDA = -3,        /* CUDA runtime failure */
+  WHIR_ERR_NO_DEVICE = -4,   /* no usable CUDA device */
+  WHIR_ERR_POW = -5,         /* proof of work exhausted its search bound */
+  WHIR_ERR_INTERNAL = -6
+} whir_status;
+
+/* Field / embedding ids, as src/bin/main.rs:84-103 dispatches AvailableFields:
+ *   GOLDILOCKS1 = Identity<Field64>, GOLDILOCKS2 = Basefield<Field64_2>,
+ *   GOLDILOCKS3 = Basefield<Field64_3> (src/algebra/fields.rs:85-143, embedding.rs:141-153). */
+enum {
+  WHIR_GOLDILOCKS1 = 0,
+  WHIR_GOLDILOCKS2 = 1,
+  WHIR_GOLDILOCKS3 = 2,
+  WHIR_FIELD192 = 4,
+  WHIR_FIELD256 = 5
+};
+
+#define WHIR_DEVICE_PTRS 1u
+
+typedef struct whir_ctx whir_ctx;
+typedef struct whir_config whir_config;
+typedef struct whir_prover_state whir_prover_state;
+typedef struct whir_witness whir_witness;
+
+/* ProtocolParameters (src/parameters.rs:9-24). hash_id is the 32-byte EngineId
+ * (src/engines.rs:22-23), e.g. Blake3 = 03e01749…5cc05b4c (src/hash/blake3_engine.rs:19). */
+typedef struct whir_params {
+  int32_t unique_decoding;
+  uint64_t starting_log_inv_rate;
+  uint64_t initial_folding_factor;
+  uint64_t folding_factor;
+  uint64_t security_level;
+  uint64_t pow_bits;
+  uint64_t batch_size;
+  uint8_t hash_id[32];
+} whir_params;
+
+const char* whir_last_error(void);
+
+/* ---- context -------------------------------------------------------------------------------- */
+int whir_ctx_create(int device, whir_ctx** out);
+int whir_ctx_destroy(whir_ctx* ctx);
+/* Blocks until all work queued on the context's stream has finished. */
+int whir_ctx_synchronize(whir_ctx* ctx);
+/* Instrumentation (no counterpart in the reference, which has no device):
+ *   whir_ctx_launch_count   kernel launches issued by this library since the context was created
+ *   whir_ctx_stream         the context's cudaStream_t (for CUDA-event timing by the caller)
+ *   whir_ctx_transfer_bytes cumulative host->device / device->host bytes moved by the context
+ *   whir_ctx_set_profiling  enable CUDA-event timing of kernel families (resets the counters)
+ *   whir_ctx_profile        per-family milliseconds and call counts; returns the number of
+ *                           families: 0 encode, 1 merkle, 2 sumcheck, 3 eq, 4 geometric, 5 lift,
+ *                           6 pow, 7 gather, 8 univariate */
+uint64_t whir_ctx_launch_count(const whir_ctx* ctx);
+void* whir_ctx_stream(const whir_ctx* ctx);
+int whir_ctx_transfer_bytes(const whir_ctx* ctx, uint64_t* h2d_bytes, uint64_t* d2h_bytes);
+int whir_ctx_set_profiling(whir_ctx* ctx, int enabled);
+int whir_ctx_profile(whir_ctx* ctx, double* ms, uint64_t* calls, size_t n_families);
+/* Device allocation helpers on the context's stream-ordered pool (for callers that keep inputs
+ * resident in HBM between calls). */
+int whir_device_alloc(whir_ctx* ctx, size_t bytes, void** out);
+int whir_device_free(whir_ctx* ctx, void* ptr);
+int whir_memcpy_h2d(whir_ctx* ctx, void* dst, const void* src, size_t bytes);
+int whir_memcpy_d2h(whir_ctx* ctx, void* dst, const void* src, size_t bytes);
+
+/* ---- protocol: Config / ProverState / commit / prove ------------------------------------------- */
+/* whir::Config::<M>::new(size, &params) (src/protocols/whir/config.rs:16-152). */
+int whir_config_new(int field, const whir_params* params, uint64_t size, whir_config** out);
+int whir_config_free(whir_config* cfg);
+/* JSON summary of the derived round schedule (sizes, sample counts, PoW thresholds). */
+int whir_config_json(const whir_config* cfg, char* buf, size_t cap);
+
+/* ProverState::new_std(&DomainSeparator::protocol(&config).session(&session).instance(&Empty))
+ * (src/transcript/mod.rs:110-181). */
+int whir_prover_state_new(const whir_config* cfg, const char* session, size_t session_len,
+                          whir_prover_state** out);
+int whir_prover_state_free(whir_prover_state* ps);
+/* Proof { narg_string, hints } (src/transcript/mod.rs:63-70, 235-243); pointers stay valid until
+ * the next call on the state. */
+int whir_prover_state_proof(const whir_prover_state* ps, const uint8_t** narg, size_t* narg_len,
+                            const uint8_t** hints, size_t* hints_len);
+
+/* Config::commit(&mut prover_state, &[&[Source]]) -> Witness (src/protocols/whir/mod.rs:79-92,
+ * irs_commit.rs:292-350). vectors: batch_size contiguous vectors of `size` source elements. The
+ * witness (codeword matrix and Merkle nodes) stays resident on the device. */
+int whir_commit(whir_ctx* ctx, const whir_config* cfg, whir_prover_state* ps, const uint64_t* vectors,
+                uint32_t flags, whir_witness** out);
+int whir_witness_free(whir_witness* w);
+int whir_witness_root(const whir_witness* w, uint8_t root[32]);
+
+/* Config::prove (src/protocols/whir/prover.rs:50-315).
+ *   vectors:     n_witnesses * batch_size contiguous vectors (same order as the witnesses)
+ *   mle_points:  n_points points of log2(size) target elements (MultilinearExtension forms)
+ *   covectors:   n_covectors explicit covectors of `size` target elements (Covector forms,
+ *                ordered after the MLE forms)
+ *   evaluations: (n_points + n_covectors) x n_vectors target elements, row-major
+ *   eval_point_out (nullable): receives FinalClaim.evaluation_point (log2(size) elements)
+ *   rlc_out (nullable): receives FinalClaim.rlc_coefficients (n_points + n_covectors elements) */
+int whir_prove(whir_ctx* ctx, const whir_config* cfg, whir_prover_state* ps, const uint64_t* vectors,
+               uint32_t flags, whir_witness* const* witnesses, size_t n_witnesses, const uint64_t* mle_points,
+               size_t n_points, const uint64_t* covectors, size_t n_covectors, const uint64_t* evaluations,
+               uint64_t* eval_point_out, uint64_t* rlc_out);
+
+/* ---- operator-level entry points --------------------------------------------------------------- */
+/* ReedSolomon::interleaved_encode (src/algebra/ntt/mod.rs:89-99, cooley_tukey.rs:411-477) via
+ * ntt::interleaved_rs_encode (ntt/mod.rs:120-128). msgs: n_msgs x msg_len (message-major); out:
+ * codeword_len x n_msgs (row-major). Masks must be empty (mask_len == 0). */
+int whir_rs_interleaved_encode(whir_ctx* ctx, int field, const uint64_t* msgs, size_t n_msgs, size_t msg_len,
+                               const uint64_t* masks, size_t mask_len, size_t codeword_len, uint64_t* out,
+                               uint32_t flags);
+/* ReedSolomon::evaluation_points (ntt/mod.rs:82-87, cooley_tukey.rs:375-402); host computation. */
+int whir_rs_evaluation_points(int field, size_t masked_len, size_t codeword_len, const uint64_t* indices, size_t n,
+                              uint64_t* out);
+/* HashEngine::hash_many (src/hash/mod.rs:79-85) for the engine with this EngineId. */
+int whir_hash_many(whir_ctx* ctx, const uint8_t engine_id[32], size_t size, const uint8_t* in, size_t count,
+                   uint8_t* out, uint32_t flags);
+/* merkle_tree::Config::commit layer hashing (src/protocols/merkle_tree.rs:82-127): leaves (n
+ * digests) -> all 2^(L+1)-1 nodes, leaves zero-padded to 2^L, root last. */
+int whir_merkle_nodes(whir_ctx* ctx, const uint8_t engine_id[32], const uint8_t* leaves, size_t n_leaves,
+                      uint8_t* nodes_out, uint32_t flags);
+/* compute_sumcheck_polynomial (src/algebra/sumcheck.rs:12-63) for power-of-two n. */
+int whir_sumcheck_polynomial(whir_ctx* ctx, int field, const uint64_t* a, const uint64_t* b, size_t n, uint64_t* c0,
+                             uint64_t* c2, uint32_t flags);
+/* fold (src/algebra/sumcheck.rs:69-104) in place for power-of-two n; v keeps n/2 elements. */
+int whir_fold(whir_ctx* ctx, int field, uint64_t* v, size_t n, const uint64_t* weight, uint32_t flags);
+/* eval_eq (src/algebra/multilinear.rs:170-190): acc (2^nvars) += scalar * eq(point, .). */
+int whir_eval_eq(whir_ctx* ctx, int field, uint64_t* acc, const uint64_t* point, size_t nvars,
+                 const uint64_t* scalar, uint32_t flags);
+/* geometric_accumulate (src/algebra/mod.rs:154-177): acc[i] += sum_j scalars[j] * points[j]^i. */
+int whir_geometric_accumulate(whir_ctx* ctx, int field, uint64_t* acc, size_t n, const uint64_t* scalars,
+                              const uint64_t* points, size_t m, uint32_t flags);
+/* mixed_univariate_evaluate (src/algebra/mod.rs:105-129) for the embedding `field`. */
+int whir_univariate_evaluate(whir_ctx* ctx, int field, const uint64_t* coeffs, size_t n, const uint64_t* point,
+                             uint64_t* out, uint32_t flags);
+/* proof_of_work::Config::prove grinding (src/protocols/proof_of_work.rs:68-166): lowest nonce with
+ * LE-u64(H(challenge || nonce_le || 0^24)[0..8]) <= threshold. */
+int whir_pow_grind(whir_ctx* ctx, const uint8_t engine_id[32], const uint8_t challenge[32], uint64_t threshold,
+                   uint64_t* nonce);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WHIR_GB300_H */

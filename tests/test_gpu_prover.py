@@ -1,0 +1,108 @@
+"""End-to-end parity of the GPU prover: commit + prove through the C ABI produce the same Merkle roots,
+NARG string and hints as the CPU oracle prover for the same inputs, the oracle verifier (a
+restatement of whir::Config::verify) accepts every GPU proof, and the final claims agree."""
+
+import hashlib
+
+import numpy as np
+import pytest
+
+import whir_gb300 as W
+from whir_gb300.inputs import Rng, field_elements
+
+pytestmark = pytest.mark.gpu
+
+
+def statement(orc, field, nv, npts, bs, nw, cov, seed):
+    from test_oracle_pins import make_statement
+    return make_statement(orc, field, nv, npts, bs, nw, cov, seed=seed)
+
+
+def gpu_prove(ctx, field, params, nv, session, vecs, pts, covs, evals, nw):
+    cfg = W.Config(field, 1 << nv, params)
+    ps = W.ProverState(cfg, session)
+    bs = params.batch_size
+    L = W.SOURCE_LIMBS[cfg.field]
+    flat = np.ascontiguousarray(vecs, dtype=np.uint64).reshape(nw, bs * (1 << nv) * L)
+    wits = [cfg.commit(ctx, ps, flat[w]) for w in range(nw)]
+    claim = cfg.prove(ctx, ps, np.ascontiguousarray(vecs, dtype=np.uint64), wits, pts, covs, evals)
+    narg, hints = ps.proof()
+    return narg, hints, claim, [w.root() for w in wits]
+
+
+CASES = [
+    # field, nv, unique, k0, k, points, pow_bits, hash, security, batch, witnesses, rate, covector
+    ("Goldilocks2", 8, True, 2, 2, 1, 5, "Sha2", 32, 1, 1, 1, False),
+    ("Goldilocks2", 10, False, 2, 2, 2, 5, "Blake3", 32, 1, 1, 1, False),
+    ("Goldilocks3", 9, False, 3, 3, 1, 0, "Blake3", 32, 1, 1, 1, True),
+    ("Goldilocks1", 8, True, 4, 4, 0, 0, "Keccak", 32, 1, 1, 1, False),
+    ("Goldilocks1", 11, False, 3, 2, 2, 8, "Sha3", 40, 1, 1, 2, False),
+    ("Goldilocks3", 8, False, 2, 2, 1, 5, "Blake3", 32, 2, 2, 1, False),
+    ("Goldilocks2", 12, True, 4, 4, 1, 10, "Blake3", 100, 1, 1, 1, False),
+    ("Goldilocks2", 14, True, 4, 4, 0, 10, "Blake3", 60, 1, 1, 1, False),
+    ("Goldilocks2", 16, True, 4, 4, 3, 20, "Blake3", 100, 1, 1, 1, False),
+    ("Goldilocks3", 16, False, 4, 4, 2, 20, "Blake3", 100, 1, 1, 1, False),
+    ("Goldilocks2", 13, True, 1, 3, 1, 10, "Blake3", 64, 1, 1, 2, False),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=["%s-nv%d-%d" % (c[0], c[1], i) for i, c in enumerate(CASES)])
+def test_gpu_proof_equals_oracle_proof(ctx, orc, case):
+    field, nv, ud, k0, k, npts, powb, h, sec, bs, nw, rate, cov = case
+    params = W.ProtocolParameters(unique_decoding=ud, security_level=sec, pow_bits=powb, hash_id=h,
+                                  initial_folding_factor=k0, folding_factor=k, starting_log_inv_rate=rate,
+                                  batch_size=bs)
+    op = orc.make_params(unique_decoding=ud, security_level=sec, pow_bits=powb, hash_id=W.ENGINES[h],
+                         initial_folding_factor=k0, folding_factor=k, starting_log_inv_rate=rate, batch_size=bs)
+    f, vecs, pts, covs, evals = statement(orc, field, nv, npts, bs, nw, cov, seed=nv + 17)
+    session = "gpu parity %s" % field
+    narg, hints, claim, roots = gpu_prove(ctx, field, params, nv, session, vecs, pts, covs, evals, nw)
+    ref = orc.whir_prove(f, op, nv, session, vecs, pts, covs, evals)
+    assert b"".join(roots) == ref.roots
+    assert narg == ref.narg
+    assert hints == ref.hints
+    assert np.array_equal(claim.evaluation_point.reshape(-1), ref.evaluation_point)
+    assert np.array_equal(claim.rlc_coefficients.reshape(-1), ref.rlc_coefficients)
+    assert orc.whir_verify(f, op, nv, session, nw, narg, hints, pts, covs, evals)
+
+
+def test_gpu_proof_is_identical_across_runs_and_contexts(ctx, orc):
+    params = W.ProtocolParameters(unique_decoding=True, security_level=100, pow_bits=20)
+    f, vecs, pts, covs, evals = statement(orc, "Goldilocks2", 14, 1, 1, 1, False, seed=3)
+    a = gpu_prove(ctx, "Goldilocks2", params, 14, "s", vecs, pts, covs, evals, 1)
+    b = gpu_prove(ctx, "Goldilocks2", params, 14, "s", vecs, pts, covs, evals, 1)
+    ctx2 = W.Context(0)
+    c = gpu_prove(ctx2, "Goldilocks2", params, 14, "s", vecs, pts, covs, evals, 1)
+    ctx2.close()
+    assert a[0] == b[0] == c[0] and a[1] == b[1] == c[1]
+
+
+def test_d20_goldilocks2_matches_oracle(ctx, orc):
+    params = W.ProtocolParameters(unique_decoding=True, security_level=100, pow_bits=20)
+    op = orc.make_params(unique_decoding=True, security_level=100, pow_bits=20)
+    r = Rng(20)
+    vec = r.goldilocks(1 << 20).reshape(1, 1 << 20)
+    pt = field_elements("Goldilocks2", 20, rng=r).reshape(20, 2)
+    ev = orc.multilinear_extend(orc.GOLDILOCKS2, vec.reshape(-1), pt.reshape(-1))
+    narg, hints, claim, roots = gpu_prove(ctx, "Goldilocks2", params, 20, "d20", vec, [pt], [], [[ev]], 1)
+    ref = orc.whir_prove(orc.GOLDILOCKS2, op, 20, "d20", vec, [pt], [], [[ev]])
+    assert narg == ref.narg and hints == ref.hints
+    assert orc.whir_verify(orc.GOLDILOCKS2, op, 20, "d20", 1, narg, hints, [pt], [], [[ev]])
+
+
+def test_d24_goldilocks2_verifies(ctx, orc):
+    # BASELINE workload shape: d=24 Goldilocks2, Blake3, rate 1/2, k=4, unique decoding, sec 100,
+    # pow 20, one random evaluation point. The oracle verifier accepts the GPU proof, and a proof
+    # with a flipped bit is rejected.
+    params = W.ProtocolParameters(unique_decoding=True, security_level=100, pow_bits=20)
+    op = orc.make_params(unique_decoding=True, security_level=100, pow_bits=20)
+    r = Rng(2)
+    vec = r.goldilocks(1 << 24).reshape(1, 1 << 24)
+    pt = field_elements("Goldilocks2", 24, rng=r).reshape(24, 2)
+    ev = orc.multilinear_extend(orc.GOLDILOCKS2, vec.reshape(-1), pt.reshape(-1))
+    narg, hints, claim, roots = gpu_prove(ctx, "Goldilocks2", params, 24, "d24", vec, [pt], [], [[ev]], 1)
+    assert orc.whir_verify(orc.GOLDILOCKS2, op, 24, "d24", 1, narg, hints, [pt], [], [[ev]])
+    bad = bytearray(hints)
+    bad[100] ^= 4
+    assert not orc.whir_verify(orc.GOLDILOCKS2, op, 24, "d24", 1, narg, bytes(bad), [pt], [], [[ev]])
+    assert hashlib.sha256(narg).hexdigest() != hashlib.sha256(hints).hexdigest()

@@ -1,0 +1,104 @@
+// Launchers for the sm_103a kernels of the WHIR prover path. Every launcher enqueues work on the
+// given stream and returns a cudaError_t (or a negative WHIR status for unsupported shapes); none
+// of them synchronizes.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "field.cuh"
+
+namespace whir {
+
+// Process-wide count of kernel launches issued by this library (instrumentation only).
+uint64_t kernel_launches();
+void note_launch();
+
+// Powers of the 2^32-th root of unity of Goldilocks: lo[i] = w^i, hi[i] = w^(i * 2^16), i < 2^16.
+struct RootTab {
+  const uint64_t* lo;
+  const uint64_t* hi;
+};
+
+// Shape of one interleaved Reed–Solomon encode (reference cooley_tukey.rs:411-477).
+struct EncodePlan {
+  int mode;          // 0: single pass (cosets_per_cta cosets per CTA); 1: four-step (two passes)
+  int logC, logN;    // coset size and codeword length (powers of two)
+  int logC1, logC2;  // four-step split C = C1 * C2
+  int cosets_per_cta;
+  int cols_per_cta;  // four-step pass 1 width
+  size_t scratch_elems;  // intermediate elements needed by mode 1
+};
+
+// Plans an encode of n_msgs messages of msg_len elements (elem_bytes each) into codeword_len rows.
+// Returns 0, or a negative status when the shape is unsupported on the device.
+int plan_encode(size_t n_msgs, size_t msg_len, size_t codeword_len, size_t elem_bytes, EncodePlan* plan);
+
+// Encodes messages (n_msgs x msg_len, message-major) into dst (codeword_len x n_msgs, row-major).
+// When leaves != nullptr, also writes the digest of every row (canonical LE bytes of its elements)
+// with engine `hash_kind`. scratch must hold plan.scratch_elems elements.
+template <class F>
+cudaError_t launch_encode(const EncodePlan& plan, const F* src, size_t n_msgs, size_t msg_len, F* dst,
+                          uint32_t* leaves, int hash_kind, F* scratch, RootTab rt, cudaStream_t s);
+
+// Builds Merkle layers above the leaf layer in place. nodes: (2^(layers+1) - 1) digests laid out
+// [leaves (2^layers)][layer 1]...[root] (merkle_tree.rs:96-121).
+cudaError_t launch_merkle(uint32_t* nodes, int layers, int hash_kind, cudaStream_t s);
+
+// count messages of `size` bytes (size % 4 == 0) -> count digests.
+cudaError_t launch_hash_many(const uint8_t* in, size_t size, size_t count, uint8_t* out, int hash_kind,
+                             cudaStream_t s);
+
+// Searches nonces [start, start + count) and atomically lowers *best to any nonce whose digest's
+// first 8 bytes (LE) are <= threshold (proof_of_work.rs:68-166).
+cudaError_t launch_pow(const uint32_t challenge[8], uint64_t threshold, uint64_t start, uint64_t count,
+                       unsigned long long* best, int hash_kind, cudaStream_t s);
+
+// out[i*cols .. (i+1)*cols) = matrix[idx[i]*cols ..]
+template <class F>
+cudaError_t launch_gather_rows(const F* matrix, size_t cols, const uint64_t* idx, size_t n, F* out, cudaStream_t s);
+cudaError_t launch_gather_digests(const uint32_t* nodes, const uint64_t* idx, size_t n, uint32_t* out,
+                                  cudaStream_t s);
+
+// ---------------------------------------------------------------------------------------------
+// Sumcheck-side kernels (reference algebra/sumcheck.rs, multilinear.rs, algebra/mod.rs)
+// ---------------------------------------------------------------------------------------------
+// Number of partial (c0, c2) pairs written by the reduce kernels for a vector of n elements.
+size_t sumcheck_partials(size_t n);
+
+// (c0, c2) of vectors a, b of n = 2^k elements -> partials (2 elements per block)
+template <class T>
+cudaError_t launch_sumcheck_compute(const T* a, const T* b, size_t n, T* partials, size_t* nparts, cudaStream_t s);
+// Folds a, b (n elements) with weight r in place to n/2 and computes (c0, c2) of the result.
+template <class T>
+cudaError_t launch_fold_compute(T* a, T* b, size_t n, T r, T* partials, size_t* nparts, cudaStream_t s);
+// v[i] += (v[i + n/2] - v[i]) * r for i < n/2
+template <class T>
+cudaError_t launch_fold(T* v, size_t n, T r, cudaStream_t s);
+// Sums nparts (c0, c2) partials into out[0..2).
+template <class T>
+cudaError_t launch_reduce_pairs(const T* partials, size_t nparts, T* out, cudaStream_t s);
+
+// acc[i] += scalar * eq(point, i), point[0] is the most significant index bit (multilinear.rs:170-190).
+// tables: scratch of 2^ceil(nv/2) + 2^floor(nv/2) elements; point is a device array.
+template <class T>
+cudaError_t launch_eval_eq(T* acc, const T* point, int nv, T scalar, T* tables, cudaStream_t s);
+
+// acc[i] += sum_j scalars[j] * points[j]^i for i < n (algebra/mod.rs:154-177). Device arrays.
+template <class T>
+cudaError_t launch_geometric_accumulate(T* acc, size_t n, const T* scalars, const T* points, size_t m,
+                                        cudaStream_t s);
+
+// dst[i] = map(v0[i]) + sum_{j>=1} coeffs[j] * v_j[i]  (lift + mixed_scalar_mul_add, algebra/mod.rs:51-98)
+template <class T, class S>
+cudaError_t launch_lift_rlc(T* dst, const S* const* vecs, const T* coeffs, size_t nvec, size_t n, cudaStream_t s);
+
+// sum_i coeffs[i] x^i (mixed_univariate_evaluate, algebra/mod.rs:105-129) -> partials; reduce with
+// launch_reduce_singles.
+template <class T, class S>
+cudaError_t launch_univariate_eval(const S* coeffs, size_t n, T x, T* partials, size_t* nparts, cudaStream_t s);
+template <class T>
+cudaError_t launch_reduce_singles(const T* partials, size_t nparts, T* out, cudaStream_t s);
+
+}  // namespace whir

@@ -1,0 +1,568 @@
+// Host-side protocol logic of the GB300 WHIR prover: parameter selection, Fiat–Shamir transcript,
+// element codecs, query sampling and Merkle opening bookkeeping. Only O(queries) work lives here;
+// everything proportional to the polynomial size runs in the CUDA kernels.
+//
+// Parameter selection restates whir::Config::new (src/protocols/whir/config.rs:16-152) and
+// irs_commit::Config::new / rbr_* (src/protocols/irs_commit.rs:125-288, 585-630) with the same f64
+// expressions; the host compiler runs with -ffp-contract=off so no fused multiply-add changes a
+// rounding. The transcript has the reference's interaction structure (src/transcript/mod.rs) on a
+// Keccak-f[1600] duplex sponge of this library (the reference's spongefish sponge is not
+// available); its exact byte rules are documented on DuplexSponge below.
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "field.cuh"
+#include "hash.cuh"
+
+namespace whir {
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+// ---------------------------------------------------------------------------------------------
+// Engines
+// ---------------------------------------------------------------------------------------------
+static const uint8_t ENGINE_IDS[5][32] = {
+    {0x03, 0xe0, 0x17, 0x49, 0xeb, 0xcc, 0x04, 0x77, 0x92, 0x42, 0x54, 0xeb, 0x48, 0x20, 0x66, 0xb8,
+     0x64, 0xa8, 0xdd, 0x4d, 0x77, 0x25, 0x24, 0x64, 0xca, 0x6f, 0x5b, 0x6f, 0x5c, 0xc0, 0x5b, 0x4c},  // Blake3
+    {0x01, 0x8e, 0xaa, 0x24, 0x7c, 0xb8, 0x95, 0x7a, 0xb1, 0xe9, 0xfd, 0xac, 0x88, 0x54, 0x50, 0x40,
+     0x3c, 0x5e, 0x7b, 0xda, 0x1a, 0xca, 0xaa, 0x50, 0x4e, 0x4c, 0xc8, 0xf2, 0xf7, 0x6b, 0xb0, 0x76},  // SHA2
+    {0xaa, 0x80, 0x2d, 0xcd, 0xab, 0xad, 0x8e, 0xa8, 0xa1, 0x43, 0x09, 0x19, 0x89, 0x3b, 0x96, 0xc3,
+     0x0e, 0x31, 0xff, 0x57, 0x34, 0xb3, 0x85, 0x99, 0x91, 0x08, 0xaa, 0x20, 0x2d, 0x27, 0xdc, 0x12},  // SHA3
+    {0xdd, 0xd2, 0x48, 0x96, 0x4e, 0x32, 0x03, 0x12, 0xa6, 0x67, 0x75, 0xae, 0xe8, 0xe1, 0x6c, 0x88,
+     0xc9, 0x27, 0x73, 0x4b, 0xe5, 0x9a, 0xca, 0x09, 0xb7, 0xaf, 0x6d, 0xeb, 0x0a, 0xd0, 0x0e, 0x8c},  // Keccak
+    {0x09, 0x45, 0x90, 0x20, 0xf4, 0x51, 0x87, 0x4a, 0x1b, 0x39, 0x98, 0x19, 0xd0, 0x79, 0x63, 0x2c,
+     0xc0, 0xf9, 0x26, 0x3b, 0x14, 0x86, 0xc4, 0x23, 0x17, 0x3c, 0x6e, 0x15, 0xd8, 0xe2, 0xd6, 0x1d}};  // Copy
+
+inline int engine_kind(const uint8_t id[32]) {
+  for (int k = 0; k < 5; ++k)
+    if (!memcmp(id, ENGINE_IDS[k], 32)) return k;
+  return -1;
+}
+
+// Host hashing of one message (transcript domain separation, verifier-side checks, small inputs).
+inline void host_hash(int kind, const uint8_t* msg, size_t len, uint8_t out[32]);
+
+// ---------------------------------------------------------------------------------------------
+// Keccak-based helpers on the host
+// ---------------------------------------------------------------------------------------------
+inline void keccak_hash(const uint8_t* in, size_t len, size_t rate, uint8_t pad, uint8_t* out, size_t outlen) {
+  uint64_t st[25] = {0};
+  uint8_t* sb = reinterpret_cast<uint8_t*>(st);
+  size_t off = 0;
+  while (len - off >= rate) {
+    for (size_t i = 0; i < rate; ++i) sb[i] ^= in[off + i];
+    keccak_f1600(st);
+    off += rate;
+  }
+  for (size_t i = 0; i < len - off; ++i) sb[i] ^= in[off + i];
+  sb[len - off] ^= pad;
+  sb[rate - 1] ^= 0x80;
+  keccak_f1600(st);
+  size_t done = 0;
+  while (done < outlen) {
+    size_t n = std::min(rate, outlen - done);
+    memcpy(out + done, sb, n);
+    done += n;
+    if (done < outlen) keccak_f1600(st);
+  }
+}
+inline void sha3_256_host(const uint8_t* in, size_t len, uint8_t out[32]) { keccak_hash(in, len, 136, 0x06, out, 32); }
+inline void sha3_512_host(const uint8_t* in, size_t len, uint8_t out[64]) { keccak_hash(in, len, 72, 0x06, out, 64); }
+
+inline void host_hash(int kind, const uint8_t* msg, size_t len, uint8_t out[32]) {
+  if (kind == HASH_COPY) {
+    memset(out, 0, 32);
+    memcpy(out, msg, std::min<size_t>(len, 32));
+    return;
+  }
+  if (kind == HASH_SHA3) return keccak_hash(msg, len, 136, 0x06, out, 32);
+  if (kind == HASH_KECCAK) return keccak_hash(msg, len, 136, 0x01, out, 32);
+  // BLAKE3 / SHA-256 on word-aligned messages through the shared word hashers.
+  if (len % 4 != 0 || (kind == HASH_BLAKE3 && len > 1024)) throw Error(-2, "host hash: unsupported message size");
+  uint32_t o[8];
+  auto run = [&](auto& h) {
+    h.init((uint32_t)len);
+    for (size_t k = 0; k < len; k += 4)
+      h.push((uint32_t)msg[k] | ((uint32_t)msg[k + 1] << 8) | ((uint32_t)msg[k + 2] << 16) | ((uint32_t)msg[k + 3] << 24));
+    h.finish(o);
+  };
+  if (kind == HASH_BLAKE3) {
+    WordHasher<HASH_BLAKE3> h;
+    run(h);
+  } else {
+    WordHasher<HASH_SHA2> h;
+    run(h);
+  }
+  for (int i = 0; i < 8; ++i)
+    for (int b = 0; b < 4; ++b) out[4 * i + b] = (uint8_t)(o[i] >> (8 * b));
+}
+
+// ---------------------------------------------------------------------------------------------
+// Transcript
+// ---------------------------------------------------------------------------------------------
+// Duplex sponge over Keccak-f[1600], rate 136 bytes:
+//   absorb  — XOR bytes into the rate, permuting before a byte that would overflow it;
+//   squeeze — on the first squeeze after absorbing, XOR 0x01 at the current position and 0x80 at
+//             rate byte 135, permute, then read rate bytes (permuting when exhausted).
+// Initialised by absorbing protocol_id (64 bytes) then session_id (32 bytes).
+struct DuplexSponge {
+  uint64_t st[25];
+  size_t pos = 0;
+  bool squeezing = false;
+  static constexpr size_t RATE = 136;
+  DuplexSponge() { memset(st, 0, sizeof(st)); }
+  uint8_t* bytes() { return reinterpret_cast<uint8_t*>(st); }
+  void absorb(const uint8_t* in, size_t n) {
+    if (squeezing) {
+      squeezing = false;
+      pos = 0;
+    }
+    for (size_t i = 0; i < n; ++i) {
+      if (pos == RATE) {
+        keccak_f1600(st);
+        pos = 0;
+      }
+      bytes()[pos++] ^= in[i];
+    }
+  }
+  void squeeze(uint8_t* out, size_t n) {
+    if (!squeezing) {
+      if (pos == RATE) {
+        keccak_f1600(st);
+        pos = 0;
+      }
+      bytes()[pos] ^= 0x01;
+      bytes()[RATE - 1] ^= 0x80;
+      keccak_f1600(st);
+      pos = 0;
+      squeezing = true;
+    }
+    for (size_t i = 0; i < n; ++i) {
+      if (pos == RATE) {
+        keccak_f1600(st);
+        pos = 0;
+      }
+      out[i] = bytes()[pos++];
+    }
+  }
+};
+
+// ProverState: NARG string (prover messages, absorbed) plus out-of-band hints (not absorbed).
+struct Transcript {
+  DuplexSponge sponge;
+  std::vector<uint8_t> narg, hints;
+  void init(const uint8_t protocol_id[64], const uint8_t session_id[32]) {
+    sponge = DuplexSponge();
+    narg.clear();
+    hints.clear();
+    sponge.absorb(protocol_id, 64);
+    sponge.absorb(session_id, 32);
+  }
+  void prover_bytes(const uint8_t* b, size_t n) {
+    narg.insert(narg.end(), b, b + n);
+    sponge.absorb(b, n);
+  }
+  void verifier_bytes(uint8_t* out, size_t n) { sponge.squeeze(out, n); }
+  void hint_bytes(const uint8_t* b, size_t n) { hints.insert(hints.end(), b, b + n); }
+};
+
+inline std::vector<uint8_t> cbor_text(const std::string& s) {
+  std::vector<uint8_t> out;
+  size_t n = s.size();
+  if (n < 24) {
+    out.push_back((uint8_t)(0x60 | n));
+  } else if (n < 256) {
+    out.push_back(0x78);
+    out.push_back((uint8_t)n);
+  } else if (n < 65536) {
+    out.push_back(0x79);
+    out.push_back((uint8_t)(n >> 8));
+    out.push_back((uint8_t)n);
+  } else {
+    out.push_back(0x7a);
+    for (int i = 3; i >= 0; --i) out.push_back((uint8_t)(n >> (8 * i)));
+  }
+  out.insert(out.end(), s.begin(), s.end());
+  return out;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Goldilocks-family codecs (8 little-endian bytes per base coefficient)
+// ---------------------------------------------------------------------------------------------
+template <class F>
+inline void elem_bytes(const F& x, uint8_t* out) {
+  for (int d = 0; d < F::DEG; ++d) {
+    uint64_t v = x.coeff(d).v;
+    for (int i = 0; i < 8; ++i) out[8 * d + i] = (uint8_t)(v >> (8 * i));
+  }
+}
+template <class F>
+inline void send_elem(Transcript& t, const F& x) {
+  uint8_t b[8 * F::DEG];
+  elem_bytes(x, b);
+  t.prover_bytes(b, sizeof(b));
+}
+// verifier_message<F>: per base coefficient squeeze 8 + 16 bytes, little-endian, reduced mod p.
+inline Gl gl_from_bytes_mod(const uint8_t* b, size_t n) {
+  uint64_t acc = 0;
+  const uint64_t two64 = GL_EPS;
+  size_t words = (n + 7) / 8;
+  for (size_t w = words; w-- > 0;) {
+    uint64_t x = 0;
+    for (int i = 7; i >= 0; --i) {
+      size_t k = w * 8 + i;
+      x = (x << 8) | (k < n ? b[k] : 0);
+    }
+    if (x >= GL_P) x -= GL_P;
+    acc = gl_add(gl_mul(acc, two64), x);
+  }
+  return Gl{acc};
+}
+template <class F>
+inline F from_coeffs(const uint64_t* c);
+template <>
+inline Gl from_coeffs<Gl>(const uint64_t* c) { return Gl{c[0]}; }
+template <>
+inline Gl2 from_coeffs<Gl2>(const uint64_t* c) { return Gl2{c[0], c[1]}; }
+template <>
+inline Gl3 from_coeffs<Gl3>(const uint64_t* c) { return Gl3{c[0], c[1], c[2]}; }
+
+template <class F>
+inline F challenge(Transcript& t) {
+  uint64_t c[3];
+  uint8_t buf[24];
+  for (int d = 0; d < F::DEG; ++d) {
+    t.verifier_bytes(buf, 24);
+    c[d] = gl_from_bytes_mod(buf, 24).v;
+  }
+  return from_coeffs<F>(c);
+}
+template <class F>
+inline std::vector<F> geometric_challenge(Transcript& t, size_t count) {
+  if (count == 0) return {};
+  if (count == 1) return {F::one()};
+  F x = challenge<F>(t);
+  std::vector<F> r(count);
+  r[0] = F::one();
+  for (size_t i = 1; i < count; ++i) r[i] = r[i - 1] * x;
+  return r;
+}
+// challenge_indices (src/protocols/challenge_indices.rs:6-50).
+inline std::vector<uint64_t> challenge_indices(Transcript& t, uint64_t num_leaves, size_t count, bool dedup) {
+  if (count == 0) return {};
+  if (num_leaves == 0 || (num_leaves & (num_leaves - 1))) throw Error(-1, "num_leaves must be a power of two");
+  if (num_leaves == 1) return dedup ? std::vector<uint64_t>{0} : std::vector<uint64_t>(count, 0);
+  int log = 0;
+  while ((1ull << log) < num_leaves) ++log;
+  size_t sb = (size_t)(log + 7) / 8;
+  std::vector<uint8_t> ent(count * sb);
+  t.verifier_bytes(ent.data(), ent.size());
+  std::vector<uint64_t> idx(count);
+  for (size_t i = 0; i < count; ++i) {
+    uint64_t acc = 0;
+    for (size_t k = 0; k < sb; ++k) acc = (acc << 8) | ent[i * sb + k];
+    idx[i] = acc % num_leaves;
+  }
+  if (dedup) {
+    std::sort(idx.begin(), idx.end());
+    idx.erase(std::unique(idx.begin(), idx.end()), idx.end());
+  }
+  return idx;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Goldilocks roots of unity (cooley_tukey.rs:51-127): the engine order is 3 * 2^32 and
+// root(n) = 7^((p - 1) / n); extension engines use the same (lifted) roots.
+// ---------------------------------------------------------------------------------------------
+inline Gl gl_root(uint64_t n) {
+  if (n == 0) return Gl{1};
+  if ((3ull << 32) % n != 0) throw Error(-1, "Subgroup of requested order does not exist.");
+  return Gl{gl_pow(7, (GL_P - 1) / n)};
+}
+// evaluation_points with the default (transpose-permuted) order (cooley_tukey.rs:375-402).
+inline std::vector<Gl> evaluation_points(uint64_t masked_len, uint64_t codeword_len, const std::vector<uint64_t>& idx) {
+  if (masked_len > codeword_len) throw Error(-1, "masked length exceeds codeword length");
+  if (codeword_len == 0 || (codeword_len & (codeword_len - 1))) throw Error(-2, "codeword length must be a power of two");
+  uint64_t C = 1;
+  while (C < masked_len) C <<= 1;
+  uint64_t K = codeword_len / C;
+  Gl g = gl_root(codeword_len);
+  std::vector<Gl> res;
+  for (uint64_t i : idx) {
+    if (i >= codeword_len) throw Error(-1, "index out of range");
+    uint64_t e = i / C + (i % C) * K;
+    res.push_back(g.pow(e));
+  }
+  return res;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Configuration
+// ---------------------------------------------------------------------------------------------
+static constexpr double LOG2_10 = 3.32192809488736234787031942948939018;
+
+struct Params {
+  bool unique_decoding;
+  size_t starting_log_inv_rate, initial_folding_factor, folding_factor, security_level, pow_bits, batch_size;
+  uint8_t hash_id[32];
+};
+
+struct Pow {
+  uint8_t hash_id[32];
+  uint64_t threshold;
+};
+
+inline uint64_t pow_threshold(double bits) {
+  if (!(bits >= 0.0 && bits <= 60.0)) throw Error(-1, "proof-of-work difficulty outside [0, 60] bits");
+  double t = std::ceil(std::exp2(64.0 - bits));
+  if (t >= 18446744073709551615.0) return UINT64_MAX;
+  return (uint64_t)t;
+}
+
+struct Irs {
+  size_t num_vectors, vector_size, mask_length, codeword_length, interleaving_depth, num_cols, layers;
+  uint8_t hash_id[32];
+  double johnson_slack;
+  size_t in_domain_samples, out_domain_samples;
+  bool dedup;
+  double field_bits;
+  size_t message_length() const { return vector_size / interleaving_depth; }
+  size_t masked_message_length() const { return message_length() + mask_length; }
+  double rate() const { return (double)masked_message_length() / (double)codeword_length; }
+  bool unique_decoding() const { return out_domain_samples == 0 && johnson_slack == 0.0; }
+  double list_size() const { return unique_decoding() ? 1.0 : 1. / (2. * johnson_slack * std::sqrt(rate())); }
+  double rbr_queries() const {
+    double per = unique_decoding() ? (1. + rate()) / 2. : std::sqrt(rate()) + johnson_slack;
+    return (double)in_domain_samples * -std::log2(per);
+  }
+  double rbr_fold() const {
+    double lir = -std::log2(rate());
+    double lk = std::log2((double)masked_message_length());
+    double err = unique_decoding() ? lk + lir : 7. * LOG2_10 + 3.5 * lir + 2. * lk;
+    return field_bits - err;
+  }
+};
+
+inline size_t layers_for(size_t n) {
+  size_t l = 0;
+  while (((size_t)1 << l) < n) ++l;
+  return l;
+}
+
+inline Irs irs_new(double sec, bool ud, const uint8_t* hash_id, size_t nvec, size_t vsize, size_t depth, double rate,
+                   double field_bits) {
+  if (depth == 0 || vsize % depth) throw Error(-1, "vector size not divisible by interleaving depth");
+  Irs c;
+  size_t ml = vsize / depth;
+  size_t cw = (size_t)std::ceil((double)ml / rate);
+  double r = (double)ml / (double)cw;
+  double js = ud ? 0.0 : std::sqrt(r) / 20.;
+  size_t ood = 0;
+  if (!ud) {
+    double L = 1. / (2. * js * std::sqrt(r));
+    double lc2 = L * (L - 1.) / 2.;
+    double lps = field_bits - std::log2((double)(vsize - 1));
+    if (!(lps > 0.)) throw Error(-1, "field too small for out-of-domain samples");
+    ood = (size_t)std::max(std::ceil((sec + std::log2(lc2)) / lps), 1.);
+  }
+  double per = ud ? (1. + r) / 2. : std::sqrt(r) + js;
+  c.num_vectors = nvec;
+  c.vector_size = vsize;
+  c.mask_length = 0;
+  c.codeword_length = cw;
+  c.interleaving_depth = depth;
+  c.num_cols = depth * nvec;
+  c.layers = layers_for(cw);
+  memcpy(c.hash_id, hash_id, 32);
+  c.johnson_slack = js;
+  c.in_domain_samples = (size_t)std::ceil(sec / (-std::log2(per)));
+  c.out_domain_samples = ood;
+  c.dedup = false;
+  c.field_bits = field_bits;
+  return c;
+}
+
+struct Sumcheck {
+  size_t initial_size, num_rounds, mask_length;
+  Pow round_pow;
+  size_t final_size() const {
+    if (initial_size == 0 || num_rounds == 0) return initial_size;
+    size_t p = 1;
+    while (p < initial_size) p <<= 1;
+    return p >> num_rounds;
+  }
+};
+
+struct Round {
+  Irs irs;
+  Sumcheck sumcheck;
+  Pow pow;
+};
+
+struct Config {
+  int field;  // embedding id
+  Irs initial;
+  Sumcheck initial_sumcheck;
+  Pow initial_skip_pow;
+  std::vector<Round> rounds;
+  Sumcheck final_sumcheck;
+  Pow final_pow;
+  size_t size() const { return initial.vector_size; }
+};
+
+inline double field_bits_of(int field) {
+  double m = (double)GL_P;  // same rounding as the reference's limb-to-f64 conversion
+  int deg = field == 0 ? 1 : (field == 1 ? 2 : 3);
+  return std::log2(m) * (double)deg;
+}
+
+inline Pow make_pow(const uint8_t* id, double bits) {
+  Pow p;
+  memcpy(p.hash_id, id, 32);
+  p.threshold = pow_threshold(bits);
+  return p;
+}
+
+inline Config config_new(int field, size_t size, const Params& wp) {
+  if (size == 0 || (size & (size - 1))) throw Error(-1, "Only powers of two size are supported at the moment.");
+  if (field < 0 || field > 2) throw Error(-2, "field not supported by the device prover");
+  if (engine_kind(wp.hash_id) < 0) throw Error(-1, "unknown hash engine id");
+  if (wp.batch_size == 0) throw Error(-1, "batch_size must be positive");
+  Config cfg;
+  cfg.field = field;
+  const double fb = field_bits_of(field);
+  const double sec = (double)wp.security_level;
+  const double psec = (double)(wp.security_level > wp.pow_bits ? wp.security_level - wp.pow_bits : 0);
+  size_t lir = wp.starting_log_inv_rate;
+  size_t nv = layers_for(size);
+  if (wp.initial_folding_factor > nv) throw Error(-1, "initial folding factor exceeds number of variables");
+  cfg.initial = irs_new(psec, wp.unique_decoding, wp.hash_id, wp.batch_size, size, (size_t)1 << wp.initial_folding_factor,
+                        std::pow(0.5, (int)wp.starting_log_inv_rate), fb);
+  const Irs& ic = cfg.initial;
+  double start_fold_bits = std::max(sec - std::min(ic.rbr_fold(), fb - std::log2(ic.list_size()) - 1.), 0.);
+  double skip_bits = std::max(sec - (ic.rbr_fold() + std::log2((double)wp.initial_folding_factor)), 0.0);
+  size_t round = 0, ids = ic.in_domain_samples;
+  double qerr = ic.rbr_queries();
+  nv -= wp.initial_folding_factor;
+  while (nv >= wp.folding_factor) {
+    size_t rff = round == 0 ? wp.initial_folding_factor : wp.folding_factor;
+    size_t next_rate = lir + (rff - 1);
+    Round rc;
+    rc.irs = irs_new(psec, wp.unique_decoding, wp.hash_id, 1, (size_t)1 << nv, (size_t)1 << wp.folding_factor,
+                     std::pow(0.5, (int)next_rate), fb);
+    double ll = std::log2(rc.irs.list_size());
+    double comb = fb - (std::log2((double)(rc.irs.out_domain_samples + ids)) + ll + 1.);
+    double pow_bits = std::max(0., sec - std::min(qerr, comb));
+    double fold_bits = std::max(sec - std::min(rc.irs.rbr_fold(), fb - (ll + 1.)), 0.);
+    rc.sumcheck.initial_size = (size_t)1 << nv;
+    rc.sumcheck.num_rounds = wp.folding_factor;
+    rc.sumcheck.mask_length = 0;
+    rc.sumcheck.round_pow = make_pow(wp.hash_id, fold_bits);
+    rc.pow = make_pow(wp.hash_id, pow_bits);
+    ++round;
+    nv -= wp.folding_factor;
+    lir = next_rate;
+    ids = rc.irs.in_domain_samples;
+    qerr = rc.irs.rbr_queries();
+    cfg.rounds.push_back(rc);
+  }
+  double rbr = cfg.rounds.empty() ? ic.rbr_queries() : cfg.rounds.back().irs.rbr_queries();
+  cfg.initial_sumcheck.initial_size = size;
+  cfg.initial_sumcheck.num_rounds = wp.initial_folding_factor;
+  cfg.initial_sumcheck.mask_length = 0;
+  cfg.initial_sumcheck.round_pow = make_pow(wp.hash_id, start_fold_bits);
+  cfg.initial_skip_pow = make_pow(wp.hash_id, skip_bits);
+  cfg.final_sumcheck.initial_size = (size_t)1 << nv;
+  cfg.final_sumcheck.num_rounds = nv;
+  cfg.final_sumcheck.mask_length = 0;
+  cfg.final_sumcheck.round_pow = make_pow(wp.hash_id, std::max(0., sec - fb + 1.0));
+  cfg.final_pow = make_pow(wp.hash_id, std::max(0., sec - rbr));
+  return cfg;
+}
+
+// Canonical configuration bytes hashed into the protocol id (SHA3-512).
+inline std::vector<uint8_t> config_bytes(const Config& c) {
+  std::vector<uint8_t> o;
+  auto u64 = [&](uint64_t v) {
+    for (int i = 0; i < 8; ++i) o.push_back((uint8_t)(v >> (8 * i)));
+  };
+  auto bytes = [&](const uint8_t* b, size_t n) { o.insert(o.end(), b, b + n); };
+  auto irs = [&](const Irs& r) {
+    u64(r.num_vectors);
+    u64(r.vector_size);
+    u64(r.mask_length);
+    u64(r.codeword_length);
+    u64(r.interleaving_depth);
+    u64(r.num_cols);
+    bytes(r.hash_id, 32);
+    u64(r.codeword_length);
+    u64(r.layers);
+    bytes(r.hash_id, 32);
+    uint64_t js;
+    memcpy(&js, &r.johnson_slack, 8);
+    u64(js);
+    u64(r.in_domain_samples);
+    u64(r.out_domain_samples);
+    u64(r.dedup ? 1 : 0);
+  };
+  auto pow = [&](const Pow& p) {
+    bytes(p.hash_id, 32);
+    u64(p.threshold);
+  };
+  auto sc = [&](const Sumcheck& s) {
+    u64(s.initial_size);
+    pow(s.round_pow);
+    u64(s.num_rounds);
+    u64(s.mask_length);
+  };
+  const char* tag = "whir-gb300 config v1";
+  bytes(reinterpret_cast<const uint8_t*>(tag), strlen(tag));
+  u64((uint64_t)c.field);
+  irs(c.initial);
+  sc(c.initial_sumcheck);
+  pow(c.initial_skip_pow);
+  u64(c.rounds.size());
+  for (auto& r : c.rounds) {
+    irs(r.irs);
+    sc(r.sumcheck);
+    pow(r.pow);
+  }
+  sc(c.final_sumcheck);
+  pow(c.final_pow);
+  return o;
+}
+
+// Sibling digests a Merkle opening must reveal, in the order merkle_tree.rs:145-186 writes them;
+// returned as absolute node indices into the [leaves][layer 1]...[root] layout.
+inline std::vector<uint64_t> merkle_open_nodes(size_t layers, std::vector<uint64_t> idx) {
+  std::sort(idx.begin(), idx.end());
+  idx.erase(std::unique(idx.begin(), idx.end()), idx.end());
+  std::vector<uint64_t> out;
+  uint64_t off = 0, len = 1ull << layers;
+  while (len > 1) {
+    std::vector<uint64_t> next;
+    for (size_t i = 0; i < idx.size(); ++i) {
+      uint64_t a = idx[i];
+      if (i + 1 < idx.size() && idx[i + 1] == (a ^ 1)) {
+        ++i;
+      } else {
+        out.push_back(off + (a ^ 1));
+      }
+      next.push_back(a >> 1);
+    }
+    idx.swap(next);
+    off += len;
+    len >>= 1;
+  }
+  return out;
+}
+
+}  // namespace whir

@@ -1,0 +1,1241 @@
+// Device-resident WHIR prover and the C ABI (include/whir_gb300.h).
+//
+// The prover follows whir::Config::prove (src/protocols/whir/prover.rs:50-315) step for step. The
+// committed vector, the covector, every codeword and every Merkle tree stay in HBM for the whole
+// proof; the host only sees what the transcript needs: Merkle roots, sumcheck round messages
+// (c0, c2), out-of-domain values, PoW nonces, the opened rows and their authentication paths, and
+// the final (constant-size) vector.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/whir_gb300.h"
+#include "field.cuh"
+#include "hash.cuh"
+#include "kernels.hpp"
+#include "protocol.hpp"
+#include "status.hpp"
+
+using namespace whir;
+
+namespace {
+thread_local std::string g_last_error;
+
+int set_error(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define CU(call)                                                                                 \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess) throw Error(WHIR_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------
+// Context
+// ------------------------------------------------------------------------------------------------
+// Kernel families timed by the optional per-family CUDA-event profiling.
+enum ProfFamily { PF_ENCODE = 0, PF_MERKLE, PF_SUMCHECK, PF_EQ, PF_GEOMETRIC, PF_LIFT, PF_POW, PF_GATHER,
+                  PF_UNIVARIATE, PF_COUNT };
+
+struct whir_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  uint64_t* d_roots = nullptr;  // lo (2^16) then hi (2^16)
+  RootTab rt{};
+  uint8_t* h_stage = nullptr;  // pinned staging for small transfers
+  size_t h_stage_cap = 0;
+  unsigned long long* d_pow = nullptr;
+  uint64_t launches_at_create = 0;
+  uint64_t h2d_bytes = 0, d2h_bytes = 0;
+  // profiling: event pairs recorded around each kernel family on the context's stream
+  bool profiling = false;
+  std::vector<cudaEvent_t> event_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  double family_ms[PF_COUNT] = {0};
+  uint64_t family_calls[PF_COUNT] = {0};
+};
+
+namespace {
+
+cudaEvent_t take_event(whir_ctx* ctx) {
+  if (!ctx->event_pool.empty()) {
+    cudaEvent_t e = ctx->event_pool.back();
+    ctx->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  if (cudaEventCreate(&e) != cudaSuccess) throw Error(WHIR_ERR_CUDA, "cudaEventCreate failed");
+  return e;
+}
+
+// Resolves recorded event pairs into per-family milliseconds (waits for the stream).
+void resolve_profile(whir_ctx* ctx) {
+  if (ctx->pending.empty()) return;
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& p : ctx->pending) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p.second.first, p.second.second);
+    ctx->family_ms[p.first] += ms;
+    ctx->family_calls[p.first] += 1;
+    ctx->event_pool.push_back(p.second.first);
+    ctx->event_pool.push_back(p.second.second);
+  }
+  ctx->pending.clear();
+}
+
+// Records a CUDA event pair around the kernels of one family when profiling is on.
+struct ProfScope {
+  whir_ctx* ctx;
+  int fam;
+  cudaEvent_t a = nullptr, b = nullptr;
+  ProfScope(whir_ctx* c, int f) : ctx(c), fam(f) {
+    if (!ctx->profiling) return;
+    a = take_event(ctx);
+    b = take_event(ctx);
+    cudaEventRecord(a, ctx->stream);
+  }
+  ~ProfScope() {
+    if (!a) return;
+    cudaEventRecord(b, ctx->stream);
+    ctx->pending.push_back({fam, {a, b}});
+    if (ctx->pending.size() > 4096) resolve_profile(ctx);
+  }
+};
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+// Stream-ordered device buffer.
+template <class T>
+struct DBuf {
+  whir_ctx* ctx = nullptr;
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(whir_ctx* c, size_t count) : ctx(c), n(count) {
+    if (count) CU(cudaMallocAsync((void**)&p, count * sizeof(T), c->stream));
+  }
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : ctx(o.ctx), p(o.p), n(o.n) { o.p = nullptr; }
+  DBuf& operator=(DBuf&& o) noexcept {
+    release();
+    ctx = o.ctx;
+    p = o.p;
+    n = o.n;
+    o.p = nullptr;
+    return *this;
+  }
+  void release() {
+    if (p) cudaFreeAsync(p, ctx->stream);
+    p = nullptr;
+  }
+  ~DBuf() { release(); }
+};
+
+void stage_reserve(whir_ctx* ctx, size_t bytes) {
+  if (bytes <= ctx->h_stage_cap) return;
+  if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+  size_t cap = std::max<size_t>(bytes, 1 << 20);
+  CU(cudaMallocHost((void**)&ctx->h_stage, cap));
+  ctx->h_stage_cap = cap;
+}
+
+// Device -> host copy of a small result; waits for the stream.
+void d2h(whir_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  if (!bytes) return;
+  ctx->d2h_bytes += bytes;
+  stage_reserve(ctx, bytes);
+  CU(cudaMemcpyAsync(ctx->h_stage, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  memcpy(dst, ctx->h_stage, bytes);
+}
+// Host -> device copy of a small argument (stream ordered; host buffer reusable on return).
+void h2d(whir_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  if (!bytes) return;
+  ctx->h2d_bytes += bytes;
+  CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+}
+
+template <class T>
+std::vector<T> load_host(const uint64_t* p, size_t n) {
+  std::vector<T> v(n);
+  for (size_t i = 0; i < n; ++i) {
+    for (int d = 0; d < T::LIMBS; ++d)
+      if (p[i * T::LIMBS + d] >= GL_P) throw Error(WHIR_ERR_INVALID, "non-canonical field element");
+    v[i] = from_coeffs<T>(p + i * T::LIMBS);
+  }
+  return v;
+}
+template <class T>
+void store_host(const std::vector<T>& v, uint64_t* p) {
+  for (size_t i = 0; i < v.size(); ++i)
+    for (int d = 0; d < T::LIMBS; ++d) p[i * T::LIMBS + d] = v[i].coeff(d).v;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------
+// Witness: irs_commit::Witness (irs_commit.rs:95-103) with the matrix and tree in HBM.
+// ------------------------------------------------------------------------------------------------
+struct whir_witness {
+  whir_ctx* ctx = nullptr;
+  int field = 0;
+  size_t codeword_len = 0, num_cols = 0, layers = 0, elem_limbs = 0;
+  DBuf<uint64_t> matrix;  // codeword_len x num_cols elements, elem_limbs u64 each
+  DBuf<uint32_t> nodes;   // (2^(layers+1) - 1) x 8 words
+  uint8_t root[32] = {0};
+  std::vector<uint64_t> ood_points;  // target limbs
+  std::vector<uint64_t> ood_matrix;  // points x vectors, target limbs
+  size_t num_vectors(size_t t_limbs) const {
+    size_t np = ood_points.size() / t_limbs;
+    return np ? ood_matrix.size() / t_limbs / np : 0;
+  }
+};
+
+struct whir_config {
+  Config cfg;
+};
+
+struct whir_prover_state {
+  Transcript ts;
+  const whir_config* cfg = nullptr;
+};
+
+namespace {
+
+int hash_kind_or_throw(const uint8_t* id) {
+  int k = engine_kind(id);
+  if (k < 0) throw Error(WHIR_ERR_INVALID, "unknown hash engine id");
+  return k;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Proof of work on the device (proof_of_work.rs:68-166)
+// ------------------------------------------------------------------------------------------------
+uint64_t grind(whir_ctx* ctx, int kind, const uint8_t chal[32], uint64_t threshold) {
+  if (kind == HASH_COPY) throw Error(WHIR_ERR_INVALID, "Copy engine cannot hash 64-byte PoW inputs");
+  uint32_t cw[8];
+  for (int i = 0; i < 8; ++i)
+    cw[i] = (uint32_t)chal[4 * i] | ((uint32_t)chal[4 * i + 1] << 8) | ((uint32_t)chal[4 * i + 2] << 16) |
+            ((uint32_t)chal[4 * i + 3] << 24);
+  // Chunk sized to the expected work: ~4x the mean number of trials, at least 2^20.
+  double expect = 18446744073709551616.0 / ((double)threshold + 1.0);
+  uint64_t chunk = 1ull << 20;
+  while ((double)chunk < 4.0 * expect && chunk < (1ull << 30)) chunk <<= 1;
+  const uint64_t limit = 1ull << 50;
+  for (uint64_t start = 0; start < limit; start += chunk) {
+    CU(cudaMemsetAsync(ctx->d_pow, 0xff, sizeof(unsigned long long), ctx->stream));
+    {
+      ProfScope prof(ctx, PF_POW);
+      CU(launch_pow(cw, threshold, start, chunk, ctx->d_pow, kind, ctx->stream));
+    }
+    unsigned long long best;
+    d2h(ctx, &best, ctx->d_pow, sizeof(best));
+    if (best != ~0ull) return best;
+  }
+  throw Error(WHIR_ERR_POW, "Proof of Work failed to solve.");
+}
+
+void pow_prove(whir_ctx* ctx, const Pow& p, Transcript& ts) {
+  if (p.threshold == UINT64_MAX) return;
+  int kind = hash_kind_or_throw(p.hash_id);
+  uint8_t chal[32];
+  ts.verifier_bytes(chal, 32);
+  uint64_t nonce = grind(ctx, kind, chal, p.threshold);
+  uint8_t nb[8];
+  for (int i = 0; i < 8; ++i) nb[i] = (uint8_t)(nonce >> (8 * i));
+  ts.prover_bytes(nb, 8);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Interleaved RS commitment on the device (irs_commit.rs:292-350)
+// ------------------------------------------------------------------------------------------------
+template <class F>
+void encode_and_tree(whir_ctx* ctx, const F* d_msgs, size_t n_msgs, size_t msg_len, size_t codeword_len, int kind,
+                     whir_witness& w) {
+  EncodePlan plan;
+  int rc = plan_encode(n_msgs, msg_len, codeword_len, sizeof(F), &plan);
+  if (rc) throw Error(rc, "encode shape unsupported on the device");
+  if (kind == HASH_BLAKE3 && n_msgs * sizeof(F) > 1024)
+    throw Error(WHIR_ERR_UNSUPPORTED, "Blake3 leaves longer than one chunk (1024 bytes) are not supported on the device");
+  if (kind == HASH_COPY && n_msgs * sizeof(F) > 32) throw Error(WHIR_ERR_INVALID, "Copy engine needs leaves <= 32 bytes");
+  w.codeword_len = codeword_len;
+  w.num_cols = n_msgs;
+  w.layers = layers_for(codeword_len);
+  w.elem_limbs = F::LIMBS;
+  w.matrix = DBuf<uint64_t>(ctx, codeword_len * n_msgs * F::LIMBS);
+  w.nodes = DBuf<uint32_t>(ctx, ((2ull << w.layers) - 1) * 8);
+  DBuf<F> scratch(ctx, plan.scratch_elems);
+  {
+    ProfScope prof(ctx, PF_ENCODE);
+    CU(launch_encode<F>(plan, d_msgs, n_msgs, msg_len, reinterpret_cast<F*>(w.matrix.p), w.nodes.p, kind, scratch.p,
+                        ctx->rt, ctx->stream));
+  }
+  {
+    ProfScope prof(ctx, PF_MERKLE);
+    CU(launch_merkle(w.nodes.p, (int)w.layers, kind, ctx->stream));
+  }
+  d2h(ctx, w.root, w.nodes.p + ((2ull << w.layers) - 2) * 8, 32);
+}
+
+template <class T, class S>
+T univariate_device(whir_ctx* ctx, const S* d_coeffs, size_t n, const T& x) {
+  DBuf<T> parts(ctx, std::max<size_t>(1, (n + 8191) / 8192) + 1);
+  size_t np = 0;
+  DBuf<T> out(ctx, 1);
+  {
+    ProfScope prof(ctx, PF_UNIVARIATE);
+    CU((launch_univariate_eval<T, S>(d_coeffs, n, x, parts.p, &np, ctx->stream)));
+    CU(launch_reduce_singles<T>(parts.p, np, out.p, ctx->stream));
+  }
+  T r;
+  d2h(ctx, &r, out.p, sizeof(T));
+  return r;
+}
+
+// vectors: num_vectors contiguous device vectors of S.
+template <class S, class T>
+std::unique_ptr<whir_witness> irs_commit(whir_ctx* ctx, const Irs& c, Transcript& ts, const S* d_vecs, int field) {
+  auto w = std::make_unique<whir_witness>();
+  w->ctx = ctx;
+  w->field = field;
+  int kind = hash_kind_or_throw(c.hash_id);
+  // Messages: each vector split into interleaving_depth contiguous chunks (irs_commit.rs:317-320),
+  // so the contiguous vector array already is the n_msgs x message_length message matrix.
+  encode_and_tree<S>(ctx, d_vecs, c.num_cols, c.message_length(), c.codeword_length, kind, *w);
+  ts.prover_bytes(w->root, 32);
+  for (size_t i = 0; i < c.out_domain_samples; ++i) {
+    T pt = challenge<T>(ts);
+    for (int d = 0; d < T::LIMBS; ++d) w->ood_points.push_back(pt.coeff(d).v);
+  }
+  for (size_t i = 0; i < c.out_domain_samples; ++i) {
+    T pt = from_coeffs<T>(&w->ood_points[i * T::LIMBS]);
+    for (size_t v = 0; v < c.num_vectors; ++v) {
+      T val = univariate_device<T, S>(ctx, d_vecs + v * c.vector_size, c.vector_size, pt);
+      send_elem<T>(ts, val);
+      for (int d = 0; d < T::LIMBS; ++d) w->ood_matrix.push_back(val.coeff(d).v);
+    }
+  }
+  return w;
+}
+
+// irs_commit::Config::open (irs_commit.rs:385-432): returns evaluation points and the opened rows
+// (points x (witnesses * num_cols)) in the witnesses' field F.
+template <class F>
+void irs_open(whir_ctx* ctx, const Irs& c, Transcript& ts, const std::vector<const whir_witness*>& ws,
+              std::vector<Gl>& points, std::vector<F>& rows) {
+  std::vector<uint64_t> idx = challenge_indices(ts, c.codeword_length, c.in_domain_samples, c.dedup);
+  points = evaluation_points(c.masked_message_length(), c.codeword_length, idx);
+  const size_t nc = c.num_cols, stride = ws.size() * nc, q = idx.size();
+  rows.assign(q * stride, F::zero());
+  std::vector<uint64_t> nodes_idx = merkle_open_nodes(c.layers, idx);
+  DBuf<uint64_t> d_idx(ctx, std::max<size_t>(q + nodes_idx.size(), 1));
+  std::vector<uint64_t> both(idx);
+  both.insert(both.end(), nodes_idx.begin(), nodes_idx.end());
+  h2d(ctx, d_idx.p, both.data(), both.size() * sizeof(uint64_t));
+  DBuf<F> d_rows(ctx, std::max<size_t>(q * nc, 1));
+  DBuf<uint32_t> d_sib(ctx, std::max<size_t>(nodes_idx.size() * 8, 1));
+  std::vector<F> sub(q * nc);
+  std::vector<uint8_t> sib(nodes_idx.size() * 32);
+  size_t off = 0;
+  for (const whir_witness* w : ws) {
+    if (w->codeword_len != c.codeword_length || w->num_cols != nc) throw Error(WHIR_ERR_INVALID, "witness shape mismatch");
+    {
+      ProfScope prof(ctx, PF_GATHER);
+      CU(launch_gather_rows<F>(reinterpret_cast<const F*>(w->matrix.p), nc, d_idx.p, q, d_rows.p, ctx->stream));
+      CU(launch_gather_digests(w->nodes.p, d_idx.p + q, nodes_idx.size(), d_sib.p, ctx->stream));
+    }
+    stage_reserve(ctx, sub.size() * sizeof(F) + sib.size());
+    ctx->d2h_bytes += sub.size() * sizeof(F) + sib.size();
+    CU(cudaMemcpyAsync(ctx->h_stage, d_rows.p, sub.size() * sizeof(F), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaMemcpyAsync(ctx->h_stage + sub.size() * sizeof(F), d_sib.p, sib.size(), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    memcpy(sub.data(), ctx->h_stage, sub.size() * sizeof(F));
+    memcpy(sib.data(), ctx->h_stage + sub.size() * sizeof(F), sib.size());
+    // prover_hint_ark(&submatrix): ark-serialize compressed Vec<F> = u64 LE length + elements.
+    uint8_t lb[8];
+    uint64_t len = sub.size();
+    for (int i = 0; i < 8; ++i) lb[i] = (uint8_t)(len >> (8 * i));
+    ts.hint_bytes(lb, 8);
+    std::vector<uint8_t> eb(sub.size() * 8 * F::DEG);
+    for (size_t i = 0; i < sub.size(); ++i) elem_bytes(sub[i], eb.data() + i * 8 * F::DEG);
+    ts.hint_bytes(eb.data(), eb.size());
+    ts.hint_bytes(sib.data(), sib.size());
+    for (size_t pi = 0; pi < q; ++pi)
+      for (size_t k = 0; k < nc; ++k) rows[pi * stride + off + k] = sub[pi * nc + k];
+    off += nc;
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Sumcheck on the device (protocols/sumcheck.rs:69-162), mask_length == 0.
+// ------------------------------------------------------------------------------------------------
+template <class T>
+struct SumcheckBuffers {
+  DBuf<T> parts, out;
+  SumcheckBuffers(whir_ctx* ctx, size_t n) : parts(ctx, 2 * sumcheck_partials(n) + 2), out(ctx, 2) {}
+};
+
+template <class T>
+std::vector<T> sumcheck_device(whir_ctx* ctx, const Sumcheck& c, Transcript& ts, T* a, T* b, size_t& n, T& sum) {
+  if (c.mask_length != 0) throw Error(WHIR_ERR_UNSUPPORTED, "masked sumcheck is not part of this prover");
+  if (n != c.initial_size) throw Error(WHIR_ERR_INTERNAL, "sumcheck size mismatch");
+  std::vector<T> rs;
+  if (c.num_rounds == 0) return rs;
+  SumcheckBuffers<T> buf(ctx, n);
+  bool have = false;
+  T prev = T::zero();
+  for (size_t round = 0; round < c.num_rounds; ++round) {
+    size_t np = 0;
+    {
+      ProfScope prof(ctx, PF_SUMCHECK);
+      if (!have) {
+        CU(launch_sumcheck_compute<T>(a, b, n, buf.parts.p, &np, ctx->stream));
+      } else {
+        CU(launch_fold_compute<T>(a, b, n, prev, buf.parts.p, &np, ctx->stream));
+        n = n > 1 ? n / 2 : n;
+      }
+      CU(launch_reduce_pairs<T>(buf.parts.p, np, buf.out.p, ctx->stream));
+    }
+    T cc[2];
+    d2h(ctx, cc, buf.out.p, sizeof(cc));
+    const T c0 = cc[0], c2 = cc[1];
+    const T c1 = sum - c0.dbl() - c2;
+    send_elem<T>(ts, c0);
+    send_elem<T>(ts, c2);
+    pow_prove(ctx, c.round_pow, ts);
+    T r = challenge<T>(ts);
+    rs.push_back(r);
+    sum = (c2 * r + c1) * r + c0;
+    prev = r;
+    have = true;
+  }
+  {
+    ProfScope prof(ctx, PF_SUMCHECK);
+    CU(launch_fold<T>(a, n, prev, ctx->stream));
+    CU(launch_fold<T>(b, n, prev, ctx->stream));
+  }
+  n = n > 1 ? n / 2 : n;
+  return rs;
+}
+
+template <class T>
+std::vector<T> eq_weights_host(const std::vector<T>& point) {
+  std::vector<T> t{T::one()};
+  for (const T& x : point) {
+    std::vector<T> nt(t.size() * 2);
+    for (size_t b = 0; b < t.size(); ++b) {
+      T s1 = t[b] * x;
+      nt[2 * b] = t[b] - s1;
+      nt[2 * b + 1] = s1;
+    }
+    t.swap(nt);
+  }
+  return t;
+}
+
+template <class T>
+T dot_host(const std::vector<T>& a, const std::vector<T>& b) {
+  T acc = T::zero();
+  for (size_t i = 0; i < a.size(); ++i) acc += a[i] * b[i];
+  return acc;
+}
+
+// ------------------------------------------------------------------------------------------------
+// whir::Config::prove on the device
+// ------------------------------------------------------------------------------------------------
+template <class S, class T>
+void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_vectors, size_t nv,
+                  const std::vector<const whir_witness*>& witnesses, const std::vector<std::vector<T>>& mle_points,
+                  const std::vector<std::vector<T>>& covectors, const std::vector<T>& evaluations,
+                  std::vector<T>& eval_point_out, std::vector<T>& rlc_out) {
+  const size_t n = cfg.size();
+  const size_t nforms = mle_points.size() + covectors.size();
+  if (nv != witnesses.size() * cfg.initial.num_vectors) throw Error(WHIR_ERR_INVALID, "vector/witness count mismatch");
+  if (evaluations.size() != nv * nforms) throw Error(WHIR_ERR_INVALID, "evaluation matrix size mismatch");
+  eval_point_out.clear();
+  rlc_out.clear();
+  if (nv == 0) return;
+
+  // Out-of-domain cross terms (prover.rs:98-128).
+  std::vector<T> oods_points, oods_matrix;
+  size_t voff = 0;
+  for (const whir_witness* w : witnesses) {
+    const size_t wn = w->num_vectors(T::LIMBS);
+    const size_t np = w->ood_points.size() / T::LIMBS;
+    for (size_t oi = 0; oi < np; ++oi) {
+      const T pt = from_coeffs<T>(&w->ood_points[oi * T::LIMBS]);
+      for (size_t j = 0; j < nv; ++j) {
+        if (j >= voff && j < voff + wn) {
+          oods_matrix.push_back(from_coeffs<T>(&w->ood_matrix[(oi * wn + (j - voff)) * T::LIMBS]));
+        } else {
+          T e = univariate_device<T, S>(ctx, d_vectors + j * n, n, pt);
+          send_elem<T>(ts, e);
+          oods_matrix.push_back(e);
+        }
+      }
+      oods_points.push_back(pt);
+    }
+    voff += wn;
+  }
+
+  std::vector<T> vector_rlc = geometric_challenge<T>(ts, nv);
+  DBuf<T> a(ctx, n), b(ctx, n);
+  {
+    std::vector<const S*> vp(nv);
+    for (size_t j = 0; j < nv; ++j) vp[j] = d_vectors + j * n;
+    ProfScope prof(ctx, PF_LIFT);
+    CU((launch_lift_rlc<T, S>(a.p, vp.data(), vector_rlc.data(), nv, n, ctx->stream)));
+  }
+  std::vector<T> constraint_rlc = geometric_challenge<T>(ts, nforms + oods_points.size());
+  const bool has_constraints = !constraint_rlc.empty();
+  std::vector<T> init_rlc(constraint_rlc.begin(), constraint_rlc.begin() + nforms);
+  std::vector<T> oods_rlc(constraint_rlc.begin() + nforms, constraint_rlc.end());
+  if (has_constraints) {
+    CU(cudaMemsetAsync(b.p, 0, n * sizeof(T), ctx->stream));
+    const int nvars = (int)layers_for(n);
+    DBuf<T> pt(ctx, std::max(nvars, 1));
+    DBuf<T> tables(ctx, (2ull << ((nvars + 1) / 2)) + 2);
+    size_t k = 0;
+    for (const auto& p : mle_points) {
+      h2d(ctx, pt.p, p.data(), p.size() * sizeof(T));
+      ProfScope prof(ctx, PF_EQ);
+      CU(launch_eval_eq<T>(b.p, pt.p, nvars, init_rlc[k], tables.p, ctx->stream));
+      ++k;
+    }
+    if (!covectors.empty()) {
+      DBuf<T> cv(ctx, n);
+      for (const auto& c : covectors) {
+        h2d(ctx, cv.p, c.data(), n * sizeof(T));
+        const T* vp = cv.p;
+        // b += rlc * covector: reuse the RLC axpy with an identity embedding.
+        std::vector<const T*> ptrs{b.p, vp};
+        std::vector<T> coeffs{T::one(), init_rlc[k]};
+        DBuf<T> tmp(ctx, n);
+        CU((launch_lift_rlc<T, T>(tmp.p, ptrs.data(), coeffs.data(), 2, n, ctx->stream)));
+        CU(cudaMemcpyAsync(b.p, tmp.p, n * sizeof(T), cudaMemcpyDeviceToDevice, ctx->stream));
+        ++k;
+      }
+    }
+  }
+  T the_sum = T::zero();
+  for (size_t f = 0; f < nforms; ++f) {
+    T row = T::zero();
+    for (size_t j = 0; j < nv; ++j) row += vector_rlc[j] * evaluations[f * nv + j];
+    the_sum += init_rlc[f] * row;
+  }
+  if (!oods_points.empty()) {
+    DBuf<T> sp(ctx, 2 * oods_points.size());
+    std::vector<T> packed(oods_rlc);
+    packed.insert(packed.end(), oods_points.begin(), oods_points.end());
+    h2d(ctx, sp.p, packed.data(), packed.size() * sizeof(T));
+    ProfScope prof(ctx, PF_GEOMETRIC);
+    CU(launch_geometric_accumulate<T>(b.p, n, sp.p, sp.p + oods_points.size(), oods_points.size(), ctx->stream));
+  }
+  for (size_t o = 0; o < oods_points.size(); ++o) {
+    T row = T::zero();
+    for (size_t j = 0; j < nv; ++j) row += vector_rlc[j] * oods_matrix[o * nv + j];
+    the_sum += oods_rlc[o] * row;
+  }
+
+  size_t len = n;  // current logical length of a and b
+  std::vector<T> folding;
+  if (has_constraints) {
+    folding = sumcheck_device<T>(ctx, cfg.initial_sumcheck, ts, a.p, b.p, len, the_sum);
+  } else {
+    for (size_t i = 0; i < cfg.initial_sumcheck.num_rounds; ++i) folding.push_back(challenge<T>(ts));
+    pow_prove(ctx, cfg.initial_skip_pow, ts);
+    for (const T& f : folding) {
+      CU(launch_fold<T>(a.p, len, f, ctx->stream));
+      len = len > 1 ? len / 2 : len;
+    }
+    CU(cudaMemsetAsync(b.p, 0, cfg.initial_sumcheck.final_size() * sizeof(T), ctx->stream));
+  }
+  std::vector<T> evaluation_point = folding;
+
+  std::unique_ptr<whir_witness> prev;
+  for (size_t ri = 0; ri < cfg.rounds.size(); ++ri) {
+    const Round& rc = cfg.rounds[ri];
+    if (len != rc.irs.vector_size) throw Error(WHIR_ERR_INTERNAL, "round vector size mismatch");
+    std::unique_ptr<whir_witness> nw = irs_commit<T, T>(ctx, rc.irs, ts, a.p, cfg.field);
+    pow_prove(ctx, rc.pow, ts);
+    std::vector<Gl> pts;
+    std::vector<T> in_rows;
+    if (!prev) {
+      std::vector<S> srows;
+      irs_open<S>(ctx, cfg.initial, ts, witnesses, pts, srows);
+      in_rows.resize(srows.size());
+      for (size_t i = 0; i < srows.size(); ++i) in_rows[i] = Embed<T, S>::map(srows[i]);
+    } else {
+      irs_open<T>(ctx, cfg.rounds[ri - 1].irs, ts, std::vector<const whir_witness*>{prev.get()}, pts, in_rows);
+    }
+    std::vector<T> stir_points;
+    std::vector<T> stir_evals;
+    const size_t nood = nw->ood_points.size() / T::LIMBS;
+    for (size_t o = 0; o < nood; ++o) {
+      stir_points.push_back(from_coeffs<T>(&nw->ood_points[o * T::LIMBS]));
+      stir_evals.push_back(from_coeffs<T>(&nw->ood_matrix[o * T::LIMBS]));
+    }
+    for (const Gl& p : pts) stir_points.push_back(T::from_base(p));
+    {
+      std::vector<T> eqw = eq_weights_host(folding);
+      std::vector<T> wts;
+      for (const T& x : vector_rlc)
+        for (const T& y : eqw) wts.push_back(x * y);
+      const size_t cols = pts.empty() ? 0 : in_rows.size() / pts.size();
+      if (cols != wts.size()) throw Error(WHIR_ERR_INTERNAL, "opened row width mismatch");
+      for (size_t pi = 0; pi < pts.size(); ++pi) {
+        T acc = T::zero();
+        for (size_t k = 0; k < cols; ++k) acc += wts[k] * in_rows[pi * cols + k];
+        stir_evals.push_back(acc);
+      }
+    }
+    std::vector<T> stir_rlc = geometric_challenge<T>(ts, stir_points.size());
+    if (!stir_points.empty()) {
+      DBuf<T> sp(ctx, 2 * stir_points.size());
+      std::vector<T> packed(stir_rlc);
+      packed.insert(packed.end(), stir_points.begin(), stir_points.end());
+      h2d(ctx, sp.p, packed.data(), packed.size() * sizeof(T));
+      ProfScope prof(ctx, PF_GEOMETRIC);
+      CU(launch_geometric_accumulate<T>(b.p, len, sp.p, sp.p + stir_points.size(), stir_points.size(), ctx->stream));
+    }
+    the_sum += dot_host(stir_rlc, stir_evals);
+    folding = sumcheck_device<T>(ctx, rc.sumcheck, ts, a.p, b.p, len, the_sum);
+    evaluation_point.insert(evaluation_point.end(), folding.begin(), folding.end());
+    prev = std::move(nw);
+    vector_rlc = {T::one()};
+  }
+
+  if (len != cfg.final_sumcheck.initial_size) throw Error(WHIR_ERR_INTERNAL, "final vector size mismatch");
+  std::vector<T> fin(len);
+  d2h(ctx, fin.data(), a.p, len * sizeof(T));
+  for (const T& x : fin) send_elem<T>(ts, x);
+  pow_prove(ctx, cfg.final_pow, ts);
+  {
+    std::vector<Gl> pts;
+    if (!prev) {
+      std::vector<S> rows;
+      irs_open<S>(ctx, cfg.initial, ts, witnesses, pts, rows);
+    } else {
+      std::vector<T> rows;
+      irs_open<T>(ctx, cfg.rounds.back().irs, ts, std::vector<const whir_witness*>{prev.get()}, pts, rows);
+    }
+  }
+  std::vector<T> last = sumcheck_device<T>(ctx, cfg.final_sumcheck, ts, a.p, b.p, len, the_sum);
+  evaluation_point.insert(evaluation_point.end(), last.begin(), last.end());
+  eval_point_out = evaluation_point;
+  rlc_out = init_rlc;
+  CU(cudaStreamSynchronize(ctx->stream));
+}
+
+// Copies host vectors to the device when needed; returns a device pointer valid for the call.
+// Small operator inputs are checked for canonical form on the host; the polynomial vectors of
+// commit/prove are taken as given (like the reference's ark-ff elements, they must be canonical).
+template <class S>
+const S* device_vectors(whir_ctx* ctx, const uint64_t* vectors, size_t count, uint32_t flags, DBuf<S>& holder,
+                        bool validate = true) {
+  if (flags & WHIR_DEVICE_PTRS) return reinterpret_cast<const S*>(vectors);
+  if (validate)
+    for (size_t i = 0; i < count * S::LIMBS; ++i)
+      if (vectors[i] >= GL_P) throw Error(WHIR_ERR_INVALID, "non-canonical field element in input vector");
+  holder = DBuf<S>(ctx, count);
+  ctx->h2d_bytes += count * sizeof(S);
+  CU(cudaMemcpyAsync(holder.p, vectors, count * sizeof(S), cudaMemcpyHostToDevice, ctx->stream));
+  return holder.p;
+}
+
+template <class Fn>
+int guarded(Fn&& fn) {
+  try {
+    return fn();
+  } catch (const Error& e) {
+    return set_error(e.code, e.what());
+  } catch (const std::bad_alloc&) {
+    return set_error(WHIR_ERR_INTERNAL, "host allocation failed");
+  } catch (const std::exception& e) {
+    return set_error(WHIR_ERR_INTERNAL, e.what());
+  }
+}
+
+int target_limbs(int field) {
+  switch (field) {
+    case WHIR_GOLDILOCKS1: return 1;
+    case WHIR_GOLDILOCKS2: return 2;
+    case WHIR_GOLDILOCKS3: return 3;
+    default: return -1;
+  }
+}
+
+// Calls f.template operator()<S, T>() for the embedding id.
+template <class Fn>
+int with_embedding(int field, Fn&& f) {
+  switch (field) {
+    case WHIR_GOLDILOCKS1: return f.template operator()<Gl, Gl>();
+    case WHIR_GOLDILOCKS2: return f.template operator()<Gl, Gl2>();
+    case WHIR_GOLDILOCKS3: return f.template operator()<Gl, Gl3>();
+    case WHIR_FIELD192:
+    case WHIR_FIELD256: throw Error(WHIR_ERR_UNSUPPORTED, "Field192/Field256 are not implemented on the device");
+    default: throw Error(WHIR_ERR_INVALID, "unknown field id");
+  }
+}
+// Calls f.template operator()<F>() for the field whose elements the operator works on.
+template <class Fn>
+int with_field(int field, Fn&& f) {
+  switch (field) {
+    case WHIR_GOLDILOCKS1: return f.template operator()<Gl>();
+    case WHIR_GOLDILOCKS2: return f.template operator()<Gl2>();
+    case WHIR_GOLDILOCKS3: return f.template operator()<Gl3>();
+    case WHIR_FIELD192:
+    case WHIR_FIELD256: throw Error(WHIR_ERR_UNSUPPORTED, "Field192/Field256 are not implemented on the device");
+    default: throw Error(WHIR_ERR_INVALID, "unknown field id");
+  }
+}
+
+void check_ctx(whir_ctx* ctx) {
+  if (!ctx) throw Error(WHIR_ERR_INVALID, "null context");
+  CU(cudaSetDevice(ctx->device));
+}
+
+}  // namespace
+
+// ================================================================================================
+// C ABI
+// ================================================================================================
+extern "C" {
+
+const char* whir_last_error(void) { return g_last_error.c_str(); }
+
+int whir_ctx_create(int device, whir_ctx** out) {
+  return guarded([&] {
+    if (!out) throw Error(WHIR_ERR_INVALID, "null output pointer");
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+      cudaGetLastError();
+      throw Error(WHIR_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    if (device < 0 || device >= count) throw Error(WHIR_ERR_INVALID, "device index out of range");
+    auto ctx = std::make_unique<whir_ctx>();
+    ctx->device = device;
+    CU(cudaSetDevice(device));
+    CU(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    // Keep freed pool memory cached across proofs.
+    cudaMemPool_t pool;
+    CU(cudaDeviceGetDefaultMemPool(&pool, device));
+    uint64_t thr = UINT64_MAX;
+    CU(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+    // Root tables: w = 7^((p-1)/2^32), lo[i] = w^i, hi[i] = w^(i 2^16).
+    std::vector<uint64_t> tab(2 << 16);
+    const uint64_t w = gl_pow(7, (GL_P - 1) >> 32);
+    const uint64_t w16 = gl_pow(w, 1ull << 16);
+    uint64_t x = 1, y = 1;
+    for (size_t i = 0; i < (1u << 16); ++i) {
+      tab[i] = x;
+      tab[(1u << 16) + i] = y;
+      x = gl_mul(x, w);
+      y = gl_mul(y, w16);
+    }
+    CU(cudaMalloc((void**)&ctx->d_roots, tab.size() * sizeof(uint64_t)));
+    CU(cudaMemcpy(ctx->d_roots, tab.data(), tab.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
+    ctx->rt.lo = ctx->d_roots;
+    ctx->rt.hi = ctx->d_roots + (1u << 16);
+    CU(cudaMalloc((void**)&ctx->d_pow, sizeof(unsigned long long)));
+    stage_reserve(ctx.get(), 1 << 20);
+    ctx->launches_at_create = kernel_launches();
+    *out = ctx.release();
+    return 0;
+  });
+}
+
+int whir_ctx_destroy(whir_ctx* ctx) {
+  if (!ctx) return 0;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& p : ctx->pending) {
+    cudaEventDestroy(p.second.first);
+    cudaEventDestroy(p.second.second);
+  }
+  for (auto e : ctx->event_pool) cudaEventDestroy(e);
+  if (ctx->d_roots) cudaFree(ctx->d_roots);
+  if (ctx->d_pow) cudaFree(ctx->d_pow);
+  if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return 0;
+}
+
+int whir_ctx_synchronize(whir_ctx* ctx) {
+  return guarded([&] {
+    check_ctx(ctx);
+    CU(cudaStreamSynchronize(ctx->stream));
+    return 0;
+  });
+}
+
+uint64_t whir_ctx_launch_count(const whir_ctx* ctx) { return ctx ? kernel_launches() - ctx->launches_at_create : 0; }
+
+void* whir_ctx_stream(const whir_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int whir_ctx_transfer_bytes(const whir_ctx* ctx, uint64_t* h2d_bytes, uint64_t* d2h_bytes) {
+  if (!ctx) return set_error(WHIR_ERR_INVALID, "null context");
+  if (h2d_bytes) *h2d_bytes = ctx->h2d_bytes;
+  if (d2h_bytes) *d2h_bytes = ctx->d2h_bytes;
+  return 0;
+}
+
+int whir_ctx_set_profiling(whir_ctx* ctx, int enabled) {
+  return guarded([&] {
+    check_ctx(ctx);
+    resolve_profile(ctx);
+    ctx->profiling = enabled != 0;
+    for (int i = 0; i < PF_COUNT; ++i) {
+      ctx->family_ms[i] = 0;
+      ctx->family_calls[i] = 0;
+    }
+    return 0;
+  });
+}
+
+int whir_ctx_profile(whir_ctx* ctx, double* ms, uint64_t* calls, size_t n_families) {
+  return guarded([&] {
+    check_ctx(ctx);
+    resolve_profile(ctx);
+    for (size_t i = 0; i < n_families && i < (size_t)PF_COUNT; ++i) {
+      if (ms) ms[i] = ctx->family_ms[i];
+      if (calls) calls[i] = ctx->family_calls[i];
+    }
+    return PF_COUNT;
+  });
+}
+
+int whir_device_alloc(whir_ctx* ctx, size_t bytes, void** out) {
+  return guarded([&] {
+    check_ctx(ctx);
+    CU(cudaMallocAsync(out, bytes, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    return 0;
+  });
+}
+int whir_device_free(whir_ctx* ctx, void* ptr) {
+  return guarded([&] {
+    check_ctx(ctx);
+    CU(cudaFreeAsync(ptr, ctx->stream));
+    return 0;
+  });
+}
+int whir_memcpy_h2d(whir_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  return guarded([&] {
+    check_ctx(ctx);
+    CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    return 0;
+  });
+}
+int whir_memcpy_d2h(whir_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  return guarded([&] {
+    check_ctx(ctx);
+    CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    return 0;
+  });
+}
+
+int whir_config_new(int field, const whir_params* p, uint64_t size, whir_config** out) {
+  return guarded([&] {
+    if (!p || !out) throw Error(WHIR_ERR_INVALID, "null argument");
+    if (field == WHIR_FIELD192 || field == WHIR_FIELD256)
+      throw Error(WHIR_ERR_UNSUPPORTED, "Field192/Field256 are not implemented on the device");
+    Params wp;
+    wp.unique_decoding = p->unique_decoding != 0;
+    wp.starting_log_inv_rate = p->starting_log_inv_rate;
+    wp.initial_folding_factor = p->initial_folding_factor;
+    wp.folding_factor = p->folding_factor;
+    wp.security_level = p->security_level;
+    wp.pow_bits = p->pow_bits;
+    wp.batch_size = p->batch_size;
+    memcpy(wp.hash_id, p->hash_id, 32);
+    auto c = std::make_unique<whir_config>();
+    c->cfg = config_new(field, size, wp);
+    *out = c.release();
+    return 0;
+  });
+}
+int whir_config_free(whir_config* cfg) {
+  delete cfg;
+  return 0;
+}
+
+int whir_config_json(const whir_config* cfg, char* buf, size_t cap) {
+  return guarded([&] {
+    if (!cfg) throw Error(WHIR_ERR_INVALID, "null config");
+    const Config& c = cfg->cfg;
+    std::string s;
+    char tmp[512];
+    auto irs = [&](const Irs& r) {
+      snprintf(tmp, sizeof(tmp),
+               "{\"num_vectors\":%zu,\"vector_size\":%zu,\"codeword_length\":%zu,\"interleaving_depth\":%zu,"
+               "\"num_cols\":%zu,\"merkle_layers\":%zu,\"in_domain_samples\":%zu,\"out_domain_samples\":%zu,"
+               "\"johnson_slack\":%.17g}",
+               r.num_vectors, r.vector_size, r.codeword_length, r.interleaving_depth, r.num_cols, r.layers,
+               r.in_domain_samples, r.out_domain_samples, r.johnson_slack);
+      s += tmp;
+    };
+    auto sc = [&](const Sumcheck& x) {
+      snprintf(tmp, sizeof(tmp), "{\"initial_size\":%zu,\"num_rounds\":%zu,\"round_pow_threshold\":%llu}",
+               x.initial_size, x.num_rounds, (unsigned long long)x.round_pow.threshold);
+      s += tmp;
+    };
+    s += "{\"initial_committer\":";
+    irs(c.initial);
+    s += ",\"initial_sumcheck\":";
+    sc(c.initial_sumcheck);
+    snprintf(tmp, sizeof(tmp), ",\"initial_skip_pow_threshold\":%llu,\"rounds\":[",
+             (unsigned long long)c.initial_skip_pow.threshold);
+    s += tmp;
+    for (size_t i = 0; i < c.rounds.size(); ++i) {
+      if (i) s += ",";
+      s += "{\"irs\":";
+      irs(c.rounds[i].irs);
+      s += ",\"sumcheck\":";
+      sc(c.rounds[i].sumcheck);
+      snprintf(tmp, sizeof(tmp), ",\"pow_threshold\":%llu}", (unsigned long long)c.rounds[i].pow.threshold);
+      s += tmp;
+    }
+    s += "],\"final_sumcheck\":";
+    sc(c.final_sumcheck);
+    snprintf(tmp, sizeof(tmp), ",\"final_pow_threshold\":%llu}", (unsigned long long)c.final_pow.threshold);
+    s += tmp;
+    if (!buf || s.size() + 1 > cap) throw Error(WHIR_ERR_INVALID, "buffer too small");
+    memcpy(buf, s.c_str(), s.size() + 1);
+    return 0;
+  });
+}
+
+int whir_prover_state_new(const whir_config* cfg, const char* session, size_t session_len, whir_prover_state** out) {
+  return guarded([&] {
+    if (!cfg || !out) throw Error(WHIR_ERR_INVALID, "null argument");
+    auto ps = std::make_unique<whir_prover_state>();
+    ps->cfg = cfg;
+    std::vector<uint8_t> cb = config_bytes(cfg->cfg);
+    uint8_t pid[64], sid[32];
+    sha3_512_host(cb.data(), cb.size(), pid);
+    std::vector<uint8_t> st = cbor_text(std::string(session ? session : "", session ? session_len : 0));
+    sha3_256_host(st.data(), st.size(), sid);
+    ps->ts.init(pid, sid);
+    *out = ps.release();
+    return 0;
+  });
+}
+int whir_prover_state_free(whir_prover_state* ps) {
+  delete ps;
+  return 0;
+}
+int whir_prover_state_proof(const whir_prover_state* ps, const uint8_t** narg, size_t* narg_len, const uint8_t** hints,
+                            size_t* hints_len) {
+  return guarded([&] {
+    if (!ps) throw Error(WHIR_ERR_INVALID, "null state");
+    if (narg) *narg = ps->ts.narg.data();
+    if (narg_len) *narg_len = ps->ts.narg.size();
+    if (hints) *hints = ps->ts.hints.data();
+    if (hints_len) *hints_len = ps->ts.hints.size();
+    return 0;
+  });
+}
+
+int whir_commit(whir_ctx* ctx, const whir_config* cfg, whir_prover_state* ps, const uint64_t* vectors, uint32_t flags,
+                whir_witness** out) {
+  return guarded([&] {
+    check_ctx(ctx);
+    if (!cfg || !ps || !vectors || !out) throw Error(WHIR_ERR_INVALID, "null argument");
+    const Config& c = cfg->cfg;
+    return with_embedding(c.field, [&]<class S, class T>() {
+      DBuf<S> holder;
+      const S* d = device_vectors<S>(ctx, vectors, c.initial.num_vectors * c.size(), flags, holder, false);
+      auto w = irs_commit<S, T>(ctx, c.initial, ps->ts, d, c.field);
+      CU(cudaStreamSynchronize(ctx->stream));
+      *out = w.release();
+      return 0;
+    });
+  });
+}
+
+int whir_witness_free(whir_witness* w) {
+  if (!w) return 0;
+  cudaSetDevice(w->ctx->device);
+  delete w;
+  return 0;
+}
+int whir_witness_root(const whir_witness* w, uint8_t root[32]) {
+  if (!w || !root) return set_error(WHIR_ERR_INVALID, "null argument");
+  memcpy(root, w->root, 32);
+  return 0;
+}
+
+int whir_prove(whir_ctx* ctx, const whir_config* cfg, whir_prover_state* ps, const uint64_t* vectors, uint32_t flags,
+               whir_witness* const* witnesses, size_t n_witnesses, const uint64_t* mle_points, size_t n_points,
+               const uint64_t* covectors, size_t n_covectors, const uint64_t* evaluations, uint64_t* eval_point_out,
+               uint64_t* rlc_out) {
+  return guarded([&] {
+    check_ctx(ctx);
+    if (!cfg || !ps) throw Error(WHIR_ERR_INVALID, "null argument");
+    const Config& c = cfg->cfg;
+    const size_t n = c.size();
+    const size_t nvars = layers_for(n);
+    const size_t nv = n_witnesses * c.initial.num_vectors;
+    const size_t nforms = n_points + n_covectors;
+    return with_embedding(c.field, [&]<class S, class T>() {
+      std::vector<const whir_witness*> ws;
+      for (size_t i = 0; i < n_witnesses; ++i) {
+        if (!witnesses || !witnesses[i]) throw Error(WHIR_ERR_INVALID, "null witness");
+        if (witnesses[i]->field != c.field || witnesses[i]->ctx != ctx) throw Error(WHIR_ERR_INVALID, "witness from another config/context");
+        ws.push_back(witnesses[i]);
+      }
+      std::vector<std::vector<T>> pts, covs;
+      for (size_t i = 0; i < n_points; ++i) pts.push_back(load_host<T>(mle_points + i * nvars * T::LIMBS, nvars));
+      for (size_t i = 0; i < n_covectors; ++i) covs.push_back(load_host<T>(covectors + i * n * T::LIMBS, n));
+      std::vector<T> evals = nforms * nv ? load_host<T>(evaluations, nforms * nv) : std::vector<T>();
+      DBuf<S> holder;
+      const S* d = nv ? device_vectors<S>(ctx, vectors, nv * n, flags, holder, false) : nullptr;
+      std::vector<T> ep, rlc;
+      prove_device<S, T>(ctx, c, ps->ts, d, nv, ws, pts, covs, evals, ep, rlc);
+      if (eval_point_out) store_host<T>(ep, eval_point_out);
+      if (rlc_out) store_host<T>(rlc, rlc_out);
+      return 0;
+    });
+  });
+}
+
+// ---- operator-level entry points ---------------------------------------------------------------
+
+int whir_rs_interleaved_encode(whir_ctx* ctx, int field, const uint64_t* msgs, size_t n_msgs, size_t msg_len,
+                               const uint64_t* masks, size_t mask_len, size_t codeword_len, uint64_t* out,
+                               uint32_t flags) {
+  return guarded([&] {
+    check_ctx(ctx);
+    (void)masks;
+    if (mask_len != 0) throw Error(WHIR_ERR_UNSUPPORTED, "masked encoding (ZK) is not part of this library");
+    if (n_msgs == 0) return 0;
+    return with_field(field, [&]<class F>() {
+      DBuf<F> in, outb;
+      const F* d_in = device_vectors<F>(ctx, msgs, n_msgs * msg_len, flags, in);
+      F* d_out = (flags & WHIR_DEVICE_PTRS) ? reinterpret_cast<F*>(out) : (outb = DBuf<F>(ctx, codeword_len * n_msgs)).p;
+      EncodePlan plan;
+      int rc = plan_encode(n_msgs, msg_len, codeword_len, sizeof(F), &plan);
+      if (rc) throw Error(rc, "encode shape unsupported on the device");
+      DBuf<F> scratch(ctx, plan.scratch_elems);
+      CU(launch_encode<F>(plan, d_in, n_msgs, msg_len, d_out, nullptr, HASH_BLAKE3, scratch.p, ctx->rt, ctx->stream));
+      if (!(flags & WHIR_DEVICE_PTRS))
+        CU(cudaMemcpyAsync(out, d_out, codeword_len * n_msgs * sizeof(F), cudaMemcpyDeviceToHost, ctx->stream));
+      CU(cudaStreamSynchronize(ctx->stream));
+      return 0;
+    });
+  });
+}
+
+int whir_rs_evaluation_points(int field, size_t masked_len, size_t codeword_len, const uint64_t* indices, size_t n,
+                              uint64_t* out) {
+  return guarded([&] {
+    int L = target_limbs(field);
+    if (L < 0) throw Error(field == WHIR_FIELD192 || field == WHIR_FIELD256 ? WHIR_ERR_UNSUPPORTED : WHIR_ERR_INVALID,
+                           "field not supported");
+    std::vector<uint64_t> idx(indices, indices + n);
+    std::vector<Gl> pts = evaluation_points(masked_len, codeword_len, idx);
+    for (size_t i = 0; i < n; ++i) {
+      out[i * L] = pts[i].v;
+      for (int d = 1; d < L; ++d) out[i * L + d] = 0;
+    }
+    return 0;
+  });
+}
+
+int whir_hash_many(whir_ctx* ctx, const uint8_t engine_id[32], size_t size, const uint8_t* in, size_t count,
+                   uint8_t* out, uint32_t flags) {
+  return guarded([&] {
+    check_ctx(ctx);
+    int kind = hash_kind_or_throw(engine_id);
+    if (kind == HASH_COPY && size > 32) throw Error(WHIR_ERR_INVALID, "Copy engine only supports sizes up to 32 bytes");
+    if (size % 4 != 0) throw Error(WHIR_ERR_UNSUPPORTED, "message sizes must be a multiple of 4 bytes on the device");
+    if (kind == HASH_BLAKE3 && size > 1024) throw Error(WHIR_ERR_UNSUPPORTED, "Blake3 messages above 1024 bytes");
+    if (count == 0) return 0;
+    DBuf<uint8_t> din, dout;
+    const uint8_t* pin = in;
+    uint8_t* pout = out;
+    if (!(flags & WHIR_DEVICE_PTRS)) {
+      din = DBuf<uint8_t>(ctx, std::max<size_t>(size * count, 1));
+      dout = DBuf<uint8_t>(ctx, 32 * count);
+      if (size) CU(cudaMemcpyAsync(din.p, in, size * count, cudaMemcpyHostToDevice, ctx->stream));
+      pin = din.p;
+      pout = dout.p;
+    }
+    CU(launch_hash_many(pin, size, count, pout, kind, ctx->stream));
+    if (!(flags & WHIR_DEVICE_PTRS)) CU(cudaMemcpyAsync(out, pout, 32 * count, cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    return 0;
+  });
+}
+
+int whir_merkle_nodes(whir_ctx* ctx, const uint8_t engine_id[32], const uint8_t* leaves, size_t n_leaves,
+                      uint8_t* nodes_out, uint32_t flags) {
+  return guarded([&] {
+    check_ctx(ctx);
+    int kind = hash_kind_or_throw(engine_id);
+    if (kind == HASH_COPY) throw Error(WHIR_ERR_INVALID, "Copy engine cannot hash 64-byte nodes");
+    const size_t layers = n_leaves ? layers_for(n_leaves) : 0;
+    const size_t nn = (2ull << layers) - 1;
+    DBuf<uint32_t> nodes(ctx, nn * 8);
+    CU(cudaMemsetAsync(nodes.p, 0, nn * 32, ctx->stream));
+    if (n_leaves)
+      CU(cudaMemcpyAsync(nodes.p, leaves, n_leaves * 32,
+                         (flags & WHIR_DEVICE_PTRS) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->stream));
+    CU(launch_merkle(nodes.p, (int)layers, kind, ctx->stream));
+    CU(cudaMemcpyAsync(nodes_out, nodes.p, nn * 32,
+                       (flags & WHIR_DEVICE_PTRS) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    return 0;
+  });
+}
+
+int whir_sumcheck_polynomial(whir_ctx* ctx, int field, const uint64_t* a, const uint64_t* b, size_t n, uint64_t* c0,
+                             uint64_t* c2, uint32_t flags) {
+  return guarded([&] {
+    check_ctx(ctx);
+    if (n && (n & (n - 1))) throw Error(WHIR_ERR_UNSUPPORTED, "length must be a power of two on the device");
+    return with_field(field, [&]<class T>() {
+      if (n == 0) {
+        for (int d = 0; d < T::LIMBS; ++d) c0[d] = c2[d] = 0;
+        return 0;
+      }
+      DBuf<T> ha, hb;
+      const T* da = device_vectors<T>(ctx, a, n, flags, ha);
+      const T* db = device_vectors<T>(ctx, b, n, flags, hb);
+      DBuf<T> parts(ctx, 2 * sumcheck_partials(n) + 2), res(ctx, 2);
+      size_t np;
+      CU(launch_sumcheck_compute<T>(da, db, n, parts.p, &np, ctx->stream));
+      CU(launch_reduce_pairs<T>(parts.p, np, res.p, ctx->stream));
+      T r[2];
+      d2h(ctx, r, res.p, sizeof(r));
+      for (int d = 0; d < T::LIMBS; ++d) {
+        c0[d] = r[0].coeff(d).v;
+        c2[d] = r[1].coeff(d).v;
+      }
+      return 0;
+    });
+  });
+}
+
+int whir_fold(whir_ctx* ctx, int field, uint64_t* v, size_t n, const uint64_t* weight, uint32_t flags) {
+  return guarded([&] {
+    check_ctx(ctx);
+    if (n && (n & (n - 1))) throw Error(WHIR_ERR_UNSUPPORTED, "length must be a power of two on the device");
+    return with_field(field, [&]<class T>() {
+      T w = load_host<T>(weight, 1)[0];
+      if (n <= 1) return 0;
+      DBuf<T> hv;
+      T* dv = (flags & WHIR_DEVICE_PTRS) ? reinterpret_cast<T*>(v) : const_cast<T*>(device_vectors<T>(ctx, v, n, flags, hv));
+      CU(launch_fold<T>(dv, n, w, ctx->stream));
+      if (!(flags & WHIR_DEVICE_PTRS)) CU(cudaMemcpyAsync(v, dv, (n / 2) * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+      CU(cudaStreamSynchronize(ctx->stream));
+      return 0;
+    });
+  });
+}
+
+int whir_eval_eq(whir_ctx* ctx, int field, uint64_t* acc, const uint64_t* point, size_t nvars, const uint64_t* scalar,
+                 uint32_t flags) {
+  return guarded([&] {
+    check_ctx(ctx);
+    return with_field(field, [&]<class T>() {
+      T s = load_host<T>(scalar, 1)[0];
+      const size_t n = 1ull << nvars;
+      DBuf<T> hacc, hpt;
+      T* dacc = (flags & WHIR_DEVICE_PTRS) ? reinterpret_cast<T*>(acc)
+                                           : const_cast<T*>(device_vectors<T>(ctx, acc, n, flags, hacc));
+      const T* dpt = nvars ? device_vectors<T>(ctx, point, nvars, flags, hpt) : nullptr;
+      DBuf<T> tables(ctx, (2ull << ((nvars + 1) / 2)) + 2);
+      if (nvars == 0) {
+        std::vector<T> one{s};
+        DBuf<T> tmp(ctx, 1);
+        h2d(ctx, tmp.p, one.data(), sizeof(T));
+        std::vector<const T*> ptrs{dacc, tmp.p};
+        std::vector<T> co{T::one(), T::one()};
+        DBuf<T> out(ctx, 1);
+        CU((launch_lift_rlc<T, T>(out.p, ptrs.data(), co.data(), 2, 1, ctx->stream)));
+        CU(cudaMemcpyAsync(dacc, out.p, sizeof(T), cudaMemcpyDeviceToDevice, ctx->stream));
+      } else {
+        CU(launch_eval_eq<T>(dacc, dpt, (int)nvars, s, tables.p, ctx->stream));
+      }
+      if (!(flags & WHIR_DEVICE_PTRS)) CU(cudaMemcpyAsync(acc, dacc, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+      CU(cudaStreamSynchronize(ctx->stream));
+      return 0;
+    });
+  });
+}
+
+int whir_geometric_accumulate(whir_ctx* ctx, int field, uint64_t* acc, size_t n, const uint64_t* scalars,
+                              const uint64_t* points, size_t m, uint32_t flags) {
+  return guarded([&] {
+    check_ctx(ctx);
+    return with_field(field, [&]<class T>() {
+      if (n == 0 || m == 0) return 0;
+      DBuf<T> hacc, hs, hp;
+      T* dacc = (flags & WHIR_DEVICE_PTRS) ? reinterpret_cast<T*>(acc)
+                                           : const_cast<T*>(device_vectors<T>(ctx, acc, n, flags, hacc));
+      const T* ds = device_vectors<T>(ctx, scalars, m, flags, hs);
+      const T* dp = device_vectors<T>(ctx, points, m, flags, hp);
+      CU(launch_geometric_accumulate<T>(dacc, n, ds, dp, m, ctx->stream));
+      if (!(flags & WHIR_DEVICE_PTRS)) CU(cudaMemcpyAsync(acc, dacc, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+      CU(cudaStreamSynchronize(ctx->stream));
+      return 0;
+    });
+  });
+}
+
+int whir_univariate_evaluate(whir_ctx* ctx, int field, const uint64_t* coeffs, size_t n, const uint64_t* point,
+                             uint64_t* out, uint32_t flags) {
+  return guarded([&] {
+    check_ctx(ctx);
+    return with_embedding(field, [&]<class S, class T>() {
+      T x = load_host<T>(point, 1)[0];
+      T r = T::zero();
+      if (n) {
+        DBuf<S> hc;
+        const S* dc = device_vectors<S>(ctx, coeffs, n, flags, hc);
+        r = univariate_device<T, S>(ctx, dc, n, x);
+      }
+      for (int d = 0; d < T::LIMBS; ++d) out[d] = r.coeff(d).v;
+      return 0;
+    });
+  });
+}
+
+int whir_pow_grind(whir_ctx* ctx, const uint8_t engine_id[32], const uint8_t challenge[32], uint64_t threshold,
+                   uint64_t* nonce) {
+  return guarded([&] {
+    check_ctx(ctx);
+    int kind = hash_kind_or_throw(engine_id);
+    *nonce = grind(ctx, kind, challenge, threshold);
+    return 0;
+  });
+}
+
+}  // extern "C"

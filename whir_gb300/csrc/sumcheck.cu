@@ -1,0 +1,365 @@
+// Sumcheck-side kernels of the WHIR prover path:
+//   sumcheck round polynomial (c0, c2) and the in-place fold, fused as fold-then-compute
+//     (reference src/algebra/sumcheck.rs:12-111, protocols/sumcheck.rs:104-155)
+//   eq-weight accumulation (multilinear.rs:170-190, linear_form/multilinear_extension.rs:38-40)
+//   geometric accumulation of STIR / OOD constraints (algebra/mod.rs:154-177)
+//   base -> extension lift and vector RLC (algebra/mod.rs:51-98)
+//   univariate (Horner) evaluation for out-of-domain samples (algebra/mod.rs:105-129)
+// Every value is an exact field element, so the reduction order inside the kernels does not
+// change any output bit relative to the reference's rayon split order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "field.cuh"
+#include "kernels.hpp"
+
+namespace whir {
+
+static constexpr int SC_THREADS = 256;
+static constexpr size_t SC_MAX_BLOCKS = 152 * 8;
+
+template <class T>
+__device__ __forceinline__ T shfl_down_t(const T& x, int d) {
+  T r;
+  const uint64_t* src = reinterpret_cast<const uint64_t*>(&x);
+  uint64_t* dst = reinterpret_cast<uint64_t*>(&r);
+#pragma unroll
+  for (int i = 0; i < (int)(sizeof(T) / 8); ++i) dst[i] = __shfl_down_sync(0xffffffffu, src[i], d);
+  return r;
+}
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T x) {
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) x = x + shfl_down_t(x, d);
+  return x;
+}
+
+// Block-wide sum; the result is valid in thread 0.
+template <class T>
+__device__ T block_sum(T x) {
+  __shared__ T part[32];
+  x = warp_sum(x);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) part[warp] = x;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  x = (threadIdx.x < nw) ? part[threadIdx.x] : T::zero();
+  if (warp == 0) x = warp_sum(x);
+  __syncthreads();
+  return x;
+}
+
+size_t sumcheck_partials(size_t n) {
+  size_t work = std::max<size_t>(n / 4, 1);
+  return std::min(SC_MAX_BLOCKS, (work + SC_THREADS - 1) / SC_THREADS);
+}
+
+template <class T>
+__global__ void __launch_bounds__(SC_THREADS) sc_compute_kernel(const T* a, const T* b, uint64_t n, T* partials) {
+  T acc0 = T::zero(), acc2 = T::zero();
+  if (n == 1) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) acc0 = a[0] * b[0];
+  } else {
+    const uint64_t h = n >> 1;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < h; i += (uint64_t)gridDim.x * blockDim.x) {
+      const T a0 = a[i], a1 = a[i + h], b0 = b[i], b1 = b[i + h];
+      acc0 += a0 * b0;
+      acc2 += (a1 - a0) * (b1 - b0);
+    }
+  }
+  acc0 = block_sum(acc0);
+  acc2 = block_sum(acc2);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = acc0;
+    partials[2 * blockIdx.x + 1] = acc2;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(SC_THREADS) sc_fold_compute_kernel(T* a, T* b, uint64_t n, T r, T* partials) {
+  T acc0 = T::zero(), acc2 = T::zero();
+  if (n <= 2) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      if (n == 2) {
+        const T fa = a[0] + (a[1] - a[0]) * r, fb = b[0] + (b[1] - b[0]) * r;
+        a[0] = fa;
+        b[0] = fb;
+        acc0 = fa * fb;
+      } else if (n == 1) {
+        acc0 = a[0] * b[0];
+      }
+    }
+  } else {
+    const uint64_t q = n >> 2, h = n >> 1;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < q; i += (uint64_t)gridDim.x * blockDim.x) {
+      const T a0 = a[i], a1 = a[i + q], a2 = a[i + h], a3 = a[i + h + q];
+      const T b0 = b[i], b1 = b[i + q], b2 = b[i + h], b3 = b[i + h + q];
+      const T fa0 = a0 + (a2 - a0) * r, fa1 = a1 + (a3 - a1) * r;
+      const T fb0 = b0 + (b2 - b0) * r, fb1 = b1 + (b3 - b1) * r;
+      a[i] = fa0;
+      a[i + q] = fa1;
+      b[i] = fb0;
+      b[i + q] = fb1;
+      acc0 += fa0 * fb0;
+      acc2 += (fa1 - fa0) * (fb1 - fb0);
+    }
+  }
+  acc0 = block_sum(acc0);
+  acc2 = block_sum(acc2);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = acc0;
+    partials[2 * blockIdx.x + 1] = acc2;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(SC_THREADS) sc_fold_kernel(T* v, uint64_t n, T r) {
+  const uint64_t h = n >> 1;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < h; i += (uint64_t)gridDim.x * blockDim.x) {
+    const T lo = v[i], hi = v[i + h];
+    v[i] = lo + (hi - lo) * r;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(SC_THREADS) reduce_pairs_kernel(const T* partials, uint64_t nparts, T* out) {
+  T s0 = T::zero(), s2 = T::zero();
+  for (uint64_t i = threadIdx.x; i < nparts; i += blockDim.x) {
+    s0 += partials[2 * i];
+    s2 += partials[2 * i + 1];
+  }
+  s0 = block_sum(s0);
+  s2 = block_sum(s2);
+  if (threadIdx.x == 0) {
+    out[0] = s0;
+    out[1] = s2;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(SC_THREADS) reduce_singles_kernel(const T* partials, uint64_t nparts, T* out) {
+  T s = T::zero();
+  for (uint64_t i = threadIdx.x; i < nparts; i += blockDim.x) s += partials[i];
+  s = block_sum(s);
+  if (threadIdx.x == 0) out[0] = s;
+}
+
+template <class T>
+cudaError_t launch_sumcheck_compute(const T* a, const T* b, size_t n, T* partials, size_t* nparts, cudaStream_t s) {
+  size_t g = sumcheck_partials(n);
+  sc_compute_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(a, b, n, partials);
+  note_launch();
+  *nparts = g;
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_fold_compute(T* a, T* b, size_t n, T r, T* partials, size_t* nparts, cudaStream_t s) {
+  size_t g = sumcheck_partials(n);
+  sc_fold_compute_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(a, b, n, r, partials);
+  note_launch();
+  *nparts = g;
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_fold(T* v, size_t n, T r, cudaStream_t s) {
+  if (n <= 1) return cudaSuccess;
+  size_t g = std::min(SC_MAX_BLOCKS, (n / 2 + SC_THREADS - 1) / SC_THREADS);
+  sc_fold_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(v, n, r);
+  note_launch();
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_reduce_pairs(const T* partials, size_t nparts, T* out, cudaStream_t s) {
+  reduce_pairs_kernel<T><<<1, SC_THREADS, 0, s>>>(partials, nparts, out);
+  note_launch();
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_reduce_singles(const T* partials, size_t nparts, T* out, cudaStream_t s) {
+  reduce_singles_kernel<T><<<1, SC_THREADS, 0, s>>>(partials, nparts, out);
+  note_launch();
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// eq weights: acc[i] += hi[i >> l] * lo[i & (2^l - 1)], hi = scalar * eq(point[0..h)),
+// lo = eq(point[h..nv)).
+// ---------------------------------------------------------------------------------------------
+template <class T>
+__global__ void eq_table_kernel(const T* point, int off, int cnt, T scalar, T* table) {
+  const uint64_t size = 1ull << cnt;
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < size; e += (uint64_t)gridDim.x * blockDim.x) {
+    T v = scalar;
+    for (int k = 0; k < cnt; ++k) {
+      const T x = point[off + k];
+      const bool bit = (e >> (cnt - 1 - k)) & 1;
+      v = v * (bit ? x : (T::one() - x));
+    }
+    table[e] = v;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(SC_THREADS) eq_accumulate_kernel(T* acc, uint64_t n, const T* hi, const T* lo, int l) {
+  const uint64_t mask = (1ull << l) - 1;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    acc[i] += hi[i >> l] * lo[i & mask];
+}
+
+template <class T>
+cudaError_t launch_eval_eq(T* acc, const T* point, int nv, T scalar, T* tables, cudaStream_t s) {
+  const int h = nv / 2, l = nv - h;
+  T* hi = tables;
+  T* lo = tables + (1ull << h);
+  eq_table_kernel<T><<<(unsigned)std::max<size_t>(1, ((1ull << h) + 255) / 256), 256, 0, s>>>(point, 0, h, scalar, hi);
+  note_launch();
+  eq_table_kernel<T><<<(unsigned)std::max<size_t>(1, ((1ull << l) + 255) / 256), 256, 0, s>>>(point, h, l, T::one(), lo);
+  note_launch();
+  const uint64_t n = 1ull << nv;
+  size_t g = std::min<size_t>(SC_MAX_BLOCKS * 2, (n + SC_THREADS - 1) / SC_THREADS);
+  eq_accumulate_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(acc, n, hi, lo, l);
+  note_launch();
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Geometric accumulation: acc[i] += sum_j s_j x_j^i. CTA covers GA_E * blockDim consecutive
+// indices; thread t handles i = base + t + u * blockDim (u < GA_E) so every access is coalesced.
+// Per point: p = s_j x_j^(base + t) then p *= x_j^blockDim per step.
+// ---------------------------------------------------------------------------------------------
+static constexpr int GA_E = 16;
+static constexpr int GA_THREADS = 256;
+static constexpr int GA_CHUNK = 64;  // points staged in shared memory at a time
+
+template <class T>
+__global__ void __launch_bounds__(GA_THREADS) geometric_kernel(T* acc, uint64_t n, const T* scalars, const T* points,
+                                                               uint64_t m) {
+  __shared__ T sA[GA_CHUNK];  // s_j * x_j^base
+  __shared__ T sB[GA_CHUNK];  // x_j^blockDim
+  __shared__ T sX[GA_CHUNK];  // x_j
+  const uint64_t base = (uint64_t)blockIdx.x * GA_THREADS * GA_E;
+  T accu[GA_E];
+#pragma unroll
+  for (int u = 0; u < GA_E; ++u) accu[u] = T::zero();
+  for (uint64_t j0 = 0; j0 < m; j0 += GA_CHUNK) {
+    const int cnt = (int)std::min<uint64_t>(GA_CHUNK, m - j0);
+    __syncthreads();
+    if (threadIdx.x < cnt) {
+      const T x = points[j0 + threadIdx.x];
+      sX[threadIdx.x] = x;
+      sA[threadIdx.x] = scalars[j0 + threadIdx.x] * x.pow(base);
+      sB[threadIdx.x] = x.pow(GA_THREADS);
+    }
+    __syncthreads();
+    for (int j = 0; j < cnt; ++j) {
+      T p = sA[j] * sX[j].pow(threadIdx.x);
+      const T stepv = sB[j];
+#pragma unroll
+      for (int u = 0; u < GA_E; ++u) {
+        accu[u] += p;
+        p = p * stepv;
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < GA_E; ++u) {
+    const uint64_t i = base + threadIdx.x + (uint64_t)u * GA_THREADS;
+    if (i < n) acc[i] += accu[u];
+  }
+}
+
+template <class T>
+cudaError_t launch_geometric_accumulate(T* acc, size_t n, const T* scalars, const T* points, size_t m, cudaStream_t s) {
+  if (m == 0 || n == 0) return cudaSuccess;
+  const size_t per = (size_t)GA_THREADS * GA_E;
+  geometric_kernel<T><<<(unsigned)((n + per - 1) / per), GA_THREADS, 0, s>>>(acc, n, scalars, points, m);
+  note_launch();
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Lift + RLC
+// ---------------------------------------------------------------------------------------------
+template <class T, class S>
+__global__ void lift_kernel(T* dst, const S* src, uint64_t n) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    dst[i] = Embed<T, S>::map(src[i]);
+}
+template <class T, class S>
+__global__ void axpy_kernel(T* dst, T c, const S* src, uint64_t n) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    dst[i] += Embed<T, S>::mul(c, src[i]);
+}
+
+template <class T, class S>
+cudaError_t launch_lift_rlc(T* dst, const S* const* vecs, const T* coeffs, size_t nvec, size_t n, cudaStream_t s) {
+  size_t g = std::min<size_t>(SC_MAX_BLOCKS * 2, (n + SC_THREADS - 1) / SC_THREADS);
+  if (g == 0) return cudaSuccess;
+  lift_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(dst, vecs[0], n);
+  note_launch();
+  for (size_t j = 1; j < nvec; ++j) {
+    axpy_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(dst, coeffs[j], vecs[j], n);
+    note_launch();
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Univariate evaluation: thread handles UE_E consecutive coefficients by Horner, scaled by
+// x^(chunk start); block sums go to partials.
+// ---------------------------------------------------------------------------------------------
+static constexpr int UE_E = 32;
+
+template <class T, class S>
+__global__ void __launch_bounds__(SC_THREADS) univariate_kernel(const S* c, uint64_t n, T x, T* partials) {
+  const uint64_t start = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * UE_E;
+  T h = T::zero();
+  if (start < n) {
+    const uint64_t end = std::min<uint64_t>(start + UE_E, n);
+    for (uint64_t i = end; i-- > start;) h = h * x + Embed<T, S>::map(c[i]);
+    h = h * x.pow(start);
+  }
+  h = block_sum(h);
+  if (threadIdx.x == 0) partials[blockIdx.x] = h;
+}
+
+template <class T, class S>
+cudaError_t launch_univariate_eval(const S* coeffs, size_t n, T x, T* partials, size_t* nparts, cudaStream_t s) {
+  size_t per = (size_t)SC_THREADS * UE_E;
+  size_t g = std::max<size_t>(1, (n + per - 1) / per);
+  univariate_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(coeffs, n, x, partials);
+  note_launch();
+  *nparts = g;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Explicit instantiations
+// ---------------------------------------------------------------------------------------------
+#define WHIR_SC_INST(T)                                                                                  \
+  template cudaError_t launch_sumcheck_compute<T>(const T*, const T*, size_t, T*, size_t*, cudaStream_t); \
+  template cudaError_t launch_fold_compute<T>(T*, T*, size_t, T, T*, size_t*, cudaStream_t);             \
+  template cudaError_t launch_fold<T>(T*, size_t, T, cudaStream_t);                                       \
+  template cudaError_t launch_reduce_pairs<T>(const T*, size_t, T*, cudaStream_t);                        \
+  template cudaError_t launch_reduce_singles<T>(const T*, size_t, T*, cudaStream_t);                      \
+  template cudaError_t launch_eval_eq<T>(T*, const T*, int, T, T*, cudaStream_t);                         \
+  template cudaError_t launch_geometric_accumulate<T>(T*, size_t, const T*, const T*, size_t, cudaStream_t);
+
+WHIR_SC_INST(Gl)
+WHIR_SC_INST(Gl2)
+WHIR_SC_INST(Gl3)
+
+template cudaError_t launch_lift_rlc<Gl, Gl>(Gl*, const Gl* const*, const Gl*, size_t, size_t, cudaStream_t);
+template cudaError_t launch_lift_rlc<Gl2, Gl>(Gl2*, const Gl* const*, const Gl2*, size_t, size_t, cudaStream_t);
+template cudaError_t launch_lift_rlc<Gl3, Gl>(Gl3*, const Gl* const*, const Gl3*, size_t, size_t, cudaStream_t);
+template cudaError_t launch_lift_rlc<Gl2, Gl2>(Gl2*, const Gl2* const*, const Gl2*, size_t, size_t, cudaStream_t);
+template cudaError_t launch_lift_rlc<Gl3, Gl3>(Gl3*, const Gl3* const*, const Gl3*, size_t, size_t, cudaStream_t);
+template cudaError_t launch_univariate_eval<Gl, Gl>(const Gl*, size_t, Gl, Gl*, size_t*, cudaStream_t);
+template cudaError_t launch_univariate_eval<Gl2, Gl>(const Gl*, size_t, Gl2, Gl2*, size_t*, cudaStream_t);
+template cudaError_t launch_univariate_eval<Gl3, Gl>(const Gl*, size_t, Gl3, Gl3*, size_t*, cudaStream_t);
+template cudaError_t launch_univariate_eval<Gl2, Gl2>(const Gl2*, size_t, Gl2, Gl2*, size_t*, cudaStream_t);
+template cudaError_t launch_univariate_eval<Gl3, Gl3>(const Gl3*, size_t, Gl3, Gl3*, size_t*, cudaStream_t);
+
+}  // namespace whir
