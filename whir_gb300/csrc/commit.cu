@@ -19,6 +19,7 @@
 #include "field.cuh"
 #include "hash.cuh"
 #include "kernels.hpp"
+#include "roots.cuh"
 #include "status.hpp"
 
 namespace whir {
@@ -31,12 +32,6 @@ static constexpr int ENC_THREADS = 256;
 static constexpr size_t ENC_SMEM_BUDGET = 64 * 1024;  // data bytes per CTA
 static constexpr int ENC_MAX_LOGN_SMEM = 12;          // largest in-CTA NTT
 
-__device__ __forceinline__ Gl root_pow(const RootTab& rt, int logn, uint64_t e) {
-  uint64_t E = e << (32 - logn);
-  return Gl{gl_mul(__ldg(rt.lo + (E & 0xFFFF)), __ldg(rt.hi + (E >> 16)))};
-}
-
-__device__ __forceinline__ uint32_t brev(uint32_t x, int bits) { return bits ? (__brev(x) >> (32 - bits)) : 0; }
 
 // In-place DIF NTT of nvec vectors of size 2^logn in shared memory; element i of vector v lives at
 // s[v*vs + i*es]. Output index k ends up at position brev(k).

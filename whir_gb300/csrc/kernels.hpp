@@ -90,6 +90,32 @@ template <class T>
 cudaError_t launch_geometric_accumulate(T* acc, size_t n, const T* scalars, const T* points, size_t m,
                                         cudaStream_t s);
 
+// acc[i] += sum_j scalars[j] * w_N^(exps[j] * i) for i < n, points given as exponents of the
+// N-th root of unity (in-domain evaluation points). Device arrays; N = 2^logN.
+template <class T>
+cudaError_t launch_geometric_roots(T* acc, size_t n, const T* scalars, const uint64_t* exps, size_t m, int logN,
+                                   RootTab rt, cudaStream_t s);
+// dense[e_k] = vals[k] for k < m (dense must be zeroed first; exponents distinct).
+template <class T>
+cudaError_t launch_scatter(T* dense, const uint64_t* idx, const T* vals, size_t m, cudaStream_t s);
+// acc[i] += src[i] for i < n
+template <class T>
+cudaError_t launch_add(T* acc, const T* src, size_t n, cudaStream_t s);
+
+// First two rounds of the initial sumcheck without materialising the lifted vector a = map(x) or
+// the covector b = sum_l eq(point_l, .) * rlc_l (tables: per form, hi (2^h) then lo (2^l) entries,
+// h = nv/2, l = nv - h, scalar folded into hi).
+template <class T, class S>
+cudaError_t launch_first_compute_eq(const S* x, size_t n, const T* tables, int nforms, int nv, T* partials,
+                                    size_t* nparts, cudaStream_t s);
+// Folds map(x) and the eq covector with r (n -> n/2) into a_out / b_out and computes (c0, c2).
+template <class T, class S>
+cudaError_t launch_first_fold_compute_eq(const S* x, size_t n, T r, const T* tables, int nforms, int nv, T* a_out,
+                                         T* b_out, T* partials, size_t* nparts, cudaStream_t s);
+// Builds the eq table of `cnt` coordinates point[off..off+cnt) scaled by scalar (device arrays).
+template <class T>
+cudaError_t launch_eq_table(const T* point, int off, int cnt, T scalar, T* table, cudaStream_t s);
+
 // dst[i] = map(v0[i]) + sum_{j>=1} coeffs[j] * v_j[i]  (lift + mixed_scalar_mul_add, algebra/mod.rs:51-98)
 template <class T, class S>
 cudaError_t launch_lift_rlc(T* dst, const S* const* vecs, const T* coeffs, size_t nvec, size_t n, cudaStream_t s);

@@ -343,9 +343,17 @@ std::unique_ptr<whir_witness> irs_commit(whir_ctx* ctx, const Irs& c, Transcript
 // (points x (witnesses * num_cols)) in the witnesses' field F.
 template <class F>
 void irs_open(whir_ctx* ctx, const Irs& c, Transcript& ts, const std::vector<const whir_witness*>& ws,
-              std::vector<Gl>& points, std::vector<F>& rows) {
+              std::vector<Gl>& points, std::vector<F>& rows, std::vector<uint64_t>* exps = nullptr) {
   std::vector<uint64_t> idx = challenge_indices(ts, c.codeword_length, c.in_domain_samples, c.dedup);
   points = evaluation_points(c.masked_message_length(), c.codeword_length, idx);
+  if (exps) {
+    // point = w_N^e with e = transpose_permute(index, K, C) (cooley_tukey.rs:391-399)
+    uint64_t C = 1;
+    while (C < c.masked_message_length()) C <<= 1;
+    const uint64_t K = c.codeword_length / C;
+    exps->clear();
+    for (uint64_t i : idx) exps->push_back(i / C + (i % C) * K);
+  }
   const size_t nc = c.num_cols, stride = ws.size() * nc, q = idx.size();
   rows.assign(q * stride, F::zero());
   std::vector<uint64_t> nodes_idx = merkle_open_nodes(c.layers, idx);
@@ -440,6 +448,112 @@ std::vector<T> sumcheck_device(whir_ctx* ctx, const Sumcheck& c, Transcript& ts,
   return rs;
 }
 
+// Initial sumcheck over a = map(x) and b = sum_l eq(point_l, .) * rlc_l without materialising
+// either at full size: round 1 computes (c0, c2) from x and the eq tables, round 2 folds on the fly
+// into the half-size buffers a_out / b_out, later rounds use the regular fold-and-compute kernel.
+// The transcript interactions are exactly those of sumcheck_device.
+template <class T, class S>
+std::vector<T> initial_sumcheck_fused(whir_ctx* ctx, const Sumcheck& c, Transcript& ts, const S* x,
+                                      const T* tables, int nforms, T* a, T* b, size_t& n, T& sum) {
+  if (c.mask_length != 0) throw Error(WHIR_ERR_UNSUPPORTED, "masked sumcheck is not part of this prover");
+  const int nvars = (int)layers_for(n);
+  std::vector<T> rs;
+  SumcheckBuffers<T> buf(ctx, n);
+  T prev = T::zero();
+  for (size_t round = 0; round < c.num_rounds; ++round) {
+    size_t np = 0;
+    {
+      ProfScope prof(ctx, PF_SUMCHECK);
+      if (round == 0) {
+        CU((launch_first_compute_eq<T, S>(x, n, tables, nforms, nvars, buf.parts.p, &np, ctx->stream)));
+      } else if (round == 1) {
+        CU((launch_first_fold_compute_eq<T, S>(x, n, prev, tables, nforms, nvars, a, b, buf.parts.p, &np,
+                                               ctx->stream)));
+        n /= 2;
+      } else {
+        CU(launch_fold_compute<T>(a, b, n, prev, buf.parts.p, &np, ctx->stream));
+        n = n > 1 ? n / 2 : n;
+      }
+      CU(launch_reduce_pairs<T>(buf.parts.p, np, buf.out.p, ctx->stream));
+    }
+    T cc[2];
+    d2h(ctx, cc, buf.out.p, sizeof(cc));
+    const T c0 = cc[0], c2 = cc[1];
+    const T c1 = sum - c0.dbl() - c2;
+    send_elem<T>(ts, c0);
+    send_elem<T>(ts, c2);
+    pow_prove(ctx, c.round_pow, ts);
+    T r = challenge<T>(ts);
+    rs.push_back(r);
+    sum = (c2 * r + c1) * r + c0;
+    prev = r;
+  }
+  {
+    ProfScope prof(ctx, PF_SUMCHECK);
+    if (c.num_rounds == 1) {
+      // Only one round: the final fold also reads x and the eq tables (its sums are unused).
+      size_t np = 0;
+      CU((launch_first_fold_compute_eq<T, S>(x, n, prev, tables, nforms, nvars, a, b, buf.parts.p, &np,
+                                             ctx->stream)));
+    } else {
+      CU(launch_fold<T>(a, n, prev, ctx->stream));
+      CU(launch_fold<T>(b, n, prev, ctx->stream));
+    }
+  }
+  n = n > 1 ? n / 2 : n;
+  return rs;
+}
+
+// covector[i] += sum_j scalars[j] * w_N^(exps[j] * i) for i < len: the STIR constraints of the
+// in-domain query points (UnivariateEvaluation::accumulate_many, linear_form/univariate_evaluation.rs
+// 26-39). Small rounds use the root-table kernel; when len * queries exceeds the cost of one size-N
+// NTT, the sum is computed as that NTT of the sparse vector S[e] = sum_{e_j = e} s_j
+// (sum_e S[e] w_N^(e i) = S's polynomial evaluated at w_N^i), of which the first len values are added.
+template <class T>
+void accumulate_in_domain(whir_ctx* ctx, T* cov, size_t len, const std::vector<T>& scalars,
+                          const std::vector<uint64_t>& exps, size_t N) {
+  if (scalars.empty() || len == 0) return;
+  const int logN = (int)layers_for(N);
+  const double direct = 3.0 * (double)len * (double)scalars.size();
+  const double ntt = (double)N * (double)(logN + 20);
+  ProfScope prof(ctx, PF_GEOMETRIC);
+  if (direct <= ntt || N < 64) {
+    DBuf<T> ds(ctx, scalars.size());
+    DBuf<uint64_t> de(ctx, exps.size());
+    h2d(ctx, ds.p, scalars.data(), scalars.size() * sizeof(T));
+    h2d(ctx, de.p, exps.data(), exps.size() * sizeof(uint64_t));
+    CU(launch_geometric_roots<T>(cov, len, ds.p, de.p, scalars.size(), logN, ctx->rt, ctx->stream));
+    return;
+  }
+  // Combine repeated query positions (indices are sampled with replacement).
+  std::vector<std::pair<uint64_t, T>> sparse;
+  for (size_t j = 0; j < scalars.size(); ++j) sparse.push_back({exps[j] % N, scalars[j]});
+  std::sort(sparse.begin(), sparse.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
+  std::vector<uint64_t> idx;
+  std::vector<T> vals;
+  for (auto& p : sparse) {
+    if (!idx.empty() && idx.back() == p.first)
+      vals.back() += p.second;
+    else {
+      idx.push_back(p.first);
+      vals.push_back(p.second);
+    }
+  }
+  DBuf<T> dense(ctx, N), out(ctx, N);
+  DBuf<uint64_t> di(ctx, idx.size());
+  DBuf<T> dv(ctx, vals.size());
+  CU(cudaMemsetAsync(dense.p, 0, N * sizeof(T), ctx->stream));
+  h2d(ctx, di.p, idx.data(), idx.size() * sizeof(uint64_t));
+  h2d(ctx, dv.p, vals.data(), vals.size() * sizeof(T));
+  CU(launch_scatter<T>(dense.p, di.p, dv.p, idx.size(), ctx->stream));
+  EncodePlan plan;
+  int rc = plan_encode(1, N, N, sizeof(T), &plan);
+  if (rc) throw Error(rc, "NTT shape unsupported on the device");
+  DBuf<T> scratch(ctx, plan.scratch_elems);
+  CU(launch_encode<T>(plan, dense.p, 1, N, out.p, nullptr, HASH_BLAKE3, scratch.p, ctx->rt, ctx->stream));
+  CU(launch_add<T>(cov, out.p, len, ctx->stream));
+}
+
 template <class T>
 std::vector<T> eq_weights_host(const std::vector<T>& point) {
   std::vector<T> t{T::one()};
@@ -501,18 +615,38 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
   }
 
   std::vector<T> vector_rlc = geometric_challenge<T>(ts, nv);
-  DBuf<T> a(ctx, n), b(ctx, n);
-  {
+  std::vector<T> constraint_rlc = geometric_challenge<T>(ts, nforms + oods_points.size());
+  const bool has_constraints = !constraint_rlc.empty();
+  std::vector<T> init_rlc(constraint_rlc.begin(), constraint_rlc.begin() + nforms);
+  std::vector<T> oods_rlc(constraint_rlc.begin() + nforms, constraint_rlc.end());
+  // Fused path: one vector and a statement made only of multilinear-evaluation forms. The first
+  // two sumcheck rounds then read the coefficients directly and evaluate the eq covector from
+  // small tables, so neither the lifted vector nor the covector is written at full size.
+  const bool fused = has_constraints && nv == 1 && covectors.empty() && oods_points.empty() && !mle_points.empty() &&
+                     n >= 8 && cfg.initial_sumcheck.num_rounds >= 1;
+  DBuf<T> a(ctx, fused ? n / 2 : n), b(ctx, fused ? n / 2 : n);
+  if (!fused) {
     std::vector<const S*> vp(nv);
     for (size_t j = 0; j < nv; ++j) vp[j] = d_vectors + j * n;
     ProfScope prof(ctx, PF_LIFT);
     CU((launch_lift_rlc<T, S>(a.p, vp.data(), vector_rlc.data(), nv, n, ctx->stream)));
   }
-  std::vector<T> constraint_rlc = geometric_challenge<T>(ts, nforms + oods_points.size());
-  const bool has_constraints = !constraint_rlc.empty();
-  std::vector<T> init_rlc(constraint_rlc.begin(), constraint_rlc.begin() + nforms);
-  std::vector<T> oods_rlc(constraint_rlc.begin() + nforms, constraint_rlc.end());
-  if (has_constraints) {
+  DBuf<T> eq_tables;
+  if (fused) {
+    const int nvars = (int)layers_for(n);
+    const int h = nvars / 2, l = nvars - h;
+    const size_t per = (1ull << h) + (1ull << l);
+    eq_tables = DBuf<T>(ctx, per * mle_points.size());
+    DBuf<T> pt(ctx, (size_t)nvars * mle_points.size());
+    std::vector<T> allp;
+    for (const auto& p : mle_points) allp.insert(allp.end(), p.begin(), p.end());
+    h2d(ctx, pt.p, allp.data(), allp.size() * sizeof(T));
+    ProfScope prof(ctx, PF_EQ);
+    for (size_t k = 0; k < mle_points.size(); ++k) {
+      CU(launch_eq_table<T>(pt.p + k * nvars, 0, h, init_rlc[k], eq_tables.p + k * per, ctx->stream));
+      CU(launch_eq_table<T>(pt.p + k * nvars, h, l, T::one(), eq_tables.p + k * per + (1ull << h), ctx->stream));
+    }
+  } else if (has_constraints) {
     CU(cudaMemsetAsync(b.p, 0, n * sizeof(T), ctx->stream));
     const int nvars = (int)layers_for(n);
     DBuf<T> pt(ctx, std::max(nvars, 1));
@@ -561,7 +695,10 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
 
   size_t len = n;  // current logical length of a and b
   std::vector<T> folding;
-  if (has_constraints) {
+  if (fused) {
+    folding = initial_sumcheck_fused<T, S>(ctx, cfg.initial_sumcheck, ts, d_vectors, eq_tables.p,
+                                           (int)mle_points.size(), a.p, b.p, len, the_sum);
+  } else if (has_constraints) {
     folding = sumcheck_device<T>(ctx, cfg.initial_sumcheck, ts, a.p, b.p, len, the_sum);
   } else {
     for (size_t i = 0; i < cfg.initial_sumcheck.num_rounds; ++i) folding.push_back(challenge<T>(ts));
@@ -582,13 +719,16 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
     pow_prove(ctx, rc.pow, ts);
     std::vector<Gl> pts;
     std::vector<T> in_rows;
+    std::vector<uint64_t> exps;
+    const size_t prev_N = prev ? cfg.rounds[ri - 1].irs.codeword_length : cfg.initial.codeword_length;
     if (!prev) {
       std::vector<S> srows;
-      irs_open<S>(ctx, cfg.initial, ts, witnesses, pts, srows);
+      irs_open<S>(ctx, cfg.initial, ts, witnesses, pts, srows, &exps);
       in_rows.resize(srows.size());
       for (size_t i = 0; i < srows.size(); ++i) in_rows[i] = Embed<T, S>::map(srows[i]);
     } else {
-      irs_open<T>(ctx, cfg.rounds[ri - 1].irs, ts, std::vector<const whir_witness*>{prev.get()}, pts, in_rows);
+      irs_open<T>(ctx, cfg.rounds[ri - 1].irs, ts, std::vector<const whir_witness*>{prev.get()}, pts, in_rows,
+                  &exps);
     }
     std::vector<T> stir_points;
     std::vector<T> stir_evals;
@@ -612,14 +752,16 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
       }
     }
     std::vector<T> stir_rlc = geometric_challenge<T>(ts, stir_points.size());
-    if (!stir_points.empty()) {
-      DBuf<T> sp(ctx, 2 * stir_points.size());
-      std::vector<T> packed(stir_rlc);
-      packed.insert(packed.end(), stir_points.begin(), stir_points.end());
+    if (nood) {
+      // Out-of-domain points are general extension elements.
+      DBuf<T> sp(ctx, 2 * nood);
+      std::vector<T> packed(stir_rlc.begin(), stir_rlc.begin() + nood);
+      packed.insert(packed.end(), stir_points.begin(), stir_points.begin() + nood);
       h2d(ctx, sp.p, packed.data(), packed.size() * sizeof(T));
       ProfScope prof(ctx, PF_GEOMETRIC);
-      CU(launch_geometric_accumulate<T>(b.p, len, sp.p, sp.p + stir_points.size(), stir_points.size(), ctx->stream));
+      CU(launch_geometric_accumulate<T>(b.p, len, sp.p, sp.p + nood, nood, ctx->stream));
     }
+    accumulate_in_domain<T>(ctx, b.p, len, std::vector<T>(stir_rlc.begin() + nood, stir_rlc.end()), exps, prev_N);
     the_sum += dot_host(stir_rlc, stir_evals);
     folding = sumcheck_device<T>(ctx, rc.sumcheck, ts, a.p, b.p, len, the_sum);
     evaluation_point.insert(evaluation_point.end(), folding.begin(), folding.end());

@@ -13,6 +13,7 @@
 
 #include "field.cuh"
 #include "kernels.hpp"
+#include "roots.cuh"
 
 namespace whir {
 
@@ -280,6 +281,190 @@ cudaError_t launch_geometric_accumulate(T* acc, size_t n, const T* scalars, cons
 }
 
 // ---------------------------------------------------------------------------------------------
+// Geometric accumulation over in-domain points x_j = w_N^(e_j): thread t of a CTA covers
+// i = base + t + u * blockDim (u < E); p = s_j w_N^(e_j i) starts from the root tables and is
+// advanced by w_N^(e_j blockDim) (a base-field multiplier) for each u.
+// ---------------------------------------------------------------------------------------------
+static constexpr int GR_THREADS = 256;
+static constexpr int GR_CHUNK = 256;
+
+template <class T, int E>
+__global__ void __launch_bounds__(GR_THREADS) geometric_roots_kernel(T* acc, uint64_t n, const T* scalars,
+                                                                     const uint64_t* exps, uint64_t m, int logN,
+                                                                     RootTab rt) {
+  __shared__ T sS[GR_CHUNK];
+  __shared__ uint64_t sE[GR_CHUNK];
+  __shared__ uint64_t sStep[GR_CHUNK];
+  const uint64_t mask = (1ull << logN) - 1;
+  const uint64_t base = (uint64_t)blockIdx.x * GR_THREADS * E;
+  const uint64_t i0 = base + threadIdx.x;
+  T accu[E];
+#pragma unroll
+  for (int u = 0; u < E; ++u) accu[u] = T::zero();
+  for (uint64_t j0 = 0; j0 < m; j0 += GR_CHUNK) {
+    const int cnt = (int)min((uint64_t)GR_CHUNK, m - j0);
+    __syncthreads();
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+      sS[k] = scalars[j0 + k];
+      const uint64_t e = exps[j0 + k] & mask;
+      sE[k] = e;
+      sStep[k] = root_pow(rt, logN, (e * GR_THREADS) & mask).v;
+    }
+    __syncthreads();
+    for (int j = 0; j < cnt; ++j) {
+      T p = sS[j].mul_base(root_pow(rt, logN, (sE[j] * i0) & mask));
+      const Gl step = Gl{sStep[j]};
+#pragma unroll
+      for (int u = 0; u < E; ++u) {
+        accu[u] += p;
+        if (u + 1 < E) p = p.mul_base(step);
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < E; ++u) {
+    const uint64_t i = i0 + (uint64_t)u * GR_THREADS;
+    if (i < n) acc[i] += accu[u];
+  }
+}
+
+template <class T>
+cudaError_t launch_geometric_roots(T* acc, size_t n, const T* scalars, const uint64_t* exps, size_t m, int logN,
+                                   RootTab rt, cudaStream_t s) {
+  if (n == 0 || m == 0) return cudaSuccess;
+  int E = 1;
+  while (E < 8 && n / ((size_t)GR_THREADS * E * 2) >= 304) E *= 2;
+  const size_t per = (size_t)GR_THREADS * E;
+  const unsigned grid = (unsigned)((n + per - 1) / per);
+  switch (E) {
+    case 1: geometric_roots_kernel<T, 1><<<grid, GR_THREADS, 0, s>>>(acc, n, scalars, exps, m, logN, rt); break;
+    case 2: geometric_roots_kernel<T, 2><<<grid, GR_THREADS, 0, s>>>(acc, n, scalars, exps, m, logN, rt); break;
+    case 4: geometric_roots_kernel<T, 4><<<grid, GR_THREADS, 0, s>>>(acc, n, scalars, exps, m, logN, rt); break;
+    default: geometric_roots_kernel<T, 8><<<grid, GR_THREADS, 0, s>>>(acc, n, scalars, exps, m, logN, rt); break;
+  }
+  note_launch();
+  return cudaGetLastError();
+}
+
+template <class T>
+__global__ void scatter_kernel(T* dense, const uint64_t* idx, const T* vals, uint64_t m) {
+  for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < m; k += (uint64_t)gridDim.x * blockDim.x)
+    dense[idx[k]] = vals[k];
+}
+template <class T>
+cudaError_t launch_scatter(T* dense, const uint64_t* idx, const T* vals, size_t m, cudaStream_t s) {
+  if (!m) return cudaSuccess;
+  scatter_kernel<T><<<(unsigned)((m + 255) / 256), 256, 0, s>>>(dense, idx, vals, m);
+  note_launch();
+  return cudaGetLastError();
+}
+
+template <class T>
+__global__ void add_kernel(T* acc, const T* src, uint64_t n) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    acc[i] += src[i];
+}
+template <class T>
+cudaError_t launch_add(T* acc, const T* src, size_t n, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  size_t g = std::min<size_t>(SC_MAX_BLOCKS * 2, (n + SC_THREADS - 1) / SC_THREADS);
+  add_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(acc, src, n);
+  note_launch();
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_eq_table(const T* point, int off, int cnt, T scalar, T* table, cudaStream_t s) {
+  eq_table_kernel<T><<<(unsigned)std::max<size_t>(1, ((1ull << cnt) + 255) / 256), 256, 0, s>>>(point, off, cnt,
+                                                                                               scalar, table);
+  note_launch();
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Fused first sumcheck rounds: a = map(x) and b = sum_l rlc_l eq(point_l, .) are evaluated on the
+// fly from the coefficient vector and small eq tables instead of being written to HBM.
+// ---------------------------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ T eq_on_the_fly(const T* tables, int nforms, int h, int l, uint64_t i) {
+  const uint64_t hs = 1ull << h, ls = 1ull << l;
+  T v = T::zero();
+  for (int f = 0; f < nforms; ++f) {
+    const T* hi = tables + (uint64_t)f * (hs + ls);
+    v += hi[i >> l] * hi[hs + (i & (ls - 1))];
+  }
+  return v;
+}
+
+template <class T, class S>
+__global__ void __launch_bounds__(SC_THREADS) first_compute_eq_kernel(const S* x, uint64_t n, const T* tables,
+                                                                      int nforms, int h, int l, T* partials) {
+  T acc0 = T::zero(), acc2 = T::zero();
+  const uint64_t half = n >> 1;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < half; i += (uint64_t)gridDim.x * blockDim.x) {
+    const S x0 = x[i], x1 = x[i + half];
+    const T b0 = eq_on_the_fly(tables, nforms, h, l, i), b1 = eq_on_the_fly(tables, nforms, h, l, i + half);
+    acc0 += Embed<T, S>::mul(b0, x0);
+    acc2 += Embed<T, S>::mul(b1 - b0, x1 - x0);
+  }
+  acc0 = block_sum(acc0);
+  acc2 = block_sum(acc2);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = acc0;
+    partials[2 * blockIdx.x + 1] = acc2;
+  }
+}
+
+template <class T, class S>
+__global__ void __launch_bounds__(SC_THREADS) first_fold_compute_eq_kernel(const S* x, uint64_t n, T r,
+                                                                           const T* tables, int nforms, int h, int l,
+                                                                           T* a_out, T* b_out, T* partials) {
+  T acc0 = T::zero(), acc2 = T::zero();
+  const uint64_t q = n >> 2, hf = n >> 1;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < q; i += (uint64_t)gridDim.x * blockDim.x) {
+    const S x0 = x[i], x1 = x[i + q], x2 = x[i + hf], x3 = x[i + hf + q];
+    const T fa0 = Embed<T, S>::map(x0) + Embed<T, S>::mul(r, x2 - x0);
+    const T fa1 = Embed<T, S>::map(x1) + Embed<T, S>::mul(r, x3 - x1);
+    const T b0 = eq_on_the_fly(tables, nforms, h, l, i), b1 = eq_on_the_fly(tables, nforms, h, l, i + q);
+    const T b2 = eq_on_the_fly(tables, nforms, h, l, i + hf), b3 = eq_on_the_fly(tables, nforms, h, l, i + hf + q);
+    const T fb0 = b0 + (b2 - b0) * r, fb1 = b1 + (b3 - b1) * r;
+    a_out[i] = fa0;
+    a_out[i + q] = fa1;
+    b_out[i] = fb0;
+    b_out[i + q] = fb1;
+    acc0 += fa0 * fb0;
+    acc2 += (fa1 - fa0) * (fb1 - fb0);
+  }
+  acc0 = block_sum(acc0);
+  acc2 = block_sum(acc2);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = acc0;
+    partials[2 * blockIdx.x + 1] = acc2;
+  }
+}
+
+template <class T, class S>
+cudaError_t launch_first_compute_eq(const S* x, size_t n, const T* tables, int nforms, int nv, T* partials,
+                                    size_t* nparts, cudaStream_t s) {
+  size_t g = sumcheck_partials(n);
+  first_compute_eq_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(x, n, tables, nforms, nv / 2, nv - nv / 2,
+                                                                    partials);
+  note_launch();
+  *nparts = g;
+  return cudaGetLastError();
+}
+template <class T, class S>
+cudaError_t launch_first_fold_compute_eq(const S* x, size_t n, T r, const T* tables, int nforms, int nv, T* a_out,
+                                         T* b_out, T* partials, size_t* nparts, cudaStream_t s) {
+  size_t g = sumcheck_partials(n);
+  first_fold_compute_eq_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(x, n, r, tables, nforms, nv / 2,
+                                                                         nv - nv / 2, a_out, b_out, partials);
+  note_launch();
+  *nparts = g;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
 // Lift + RLC
 // ---------------------------------------------------------------------------------------------
 template <class T, class S>
@@ -345,7 +530,16 @@ cudaError_t launch_univariate_eval(const S* coeffs, size_t n, T x, T* partials, 
   template cudaError_t launch_reduce_pairs<T>(const T*, size_t, T*, cudaStream_t);                        \
   template cudaError_t launch_reduce_singles<T>(const T*, size_t, T*, cudaStream_t);                      \
   template cudaError_t launch_eval_eq<T>(T*, const T*, int, T, T*, cudaStream_t);                         \
-  template cudaError_t launch_geometric_accumulate<T>(T*, size_t, const T*, const T*, size_t, cudaStream_t);
+  template cudaError_t launch_geometric_accumulate<T>(T*, size_t, const T*, const T*, size_t, cudaStream_t);      \
+  template cudaError_t launch_geometric_roots<T>(T*, size_t, const T*, const uint64_t*, size_t, int, RootTab,    \
+                                                 cudaStream_t);                                                  \
+  template cudaError_t launch_scatter<T>(T*, const uint64_t*, const T*, size_t, cudaStream_t);                   \
+  template cudaError_t launch_add<T>(T*, const T*, size_t, cudaStream_t);                                        \
+  template cudaError_t launch_eq_table<T>(const T*, int, int, T, T*, cudaStream_t);                              \
+  template cudaError_t launch_first_compute_eq<T, Gl>(const Gl*, size_t, const T*, int, int, T*, size_t*,        \
+                                                      cudaStream_t);                                             \
+  template cudaError_t launch_first_fold_compute_eq<T, Gl>(const Gl*, size_t, T, const T*, int, int, T*, T*, T*, \
+                                                           size_t*, cudaStream_t);
 
 WHIR_SC_INST(Gl)
 WHIR_SC_INST(Gl2)
