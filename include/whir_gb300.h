@@ -167,6 +167,28 @@ int whir_univariate_evaluate(whir_ctx* ctx, int field, const uint64_t* coeffs, s
 int whir_pow_grind(whir_ctx* ctx, const uint8_t engine_id[32], const uint8_t challenge[32], uint64_t threshold,
                    uint64_t* nonce);
 
+/* ---- no-allocation variant ---------------------------------------------------------------------
+ * No counterpart in the reference. eval_eq (acc += scalar * eq(point, .)) for callers that cannot
+ * call cudaMalloc where they need it: code inside a CUDA stream capture, hosts that embed the
+ * prover behind an allocator they do not control, callers with a fixed device-memory budget. It
+ * needs no whir_ctx and allocates nothing: acc_dev (2^nvars elements) and point_dev (nvars
+ * elements) are caller-owned device buffers on the current device, scalar is one host element,
+ * stream is a cudaStream_t (NULL = legacy default stream); the work is only enqueued.
+ *   - Scratch: the two eq tables live in one file-scope device array of
+ *     whir_eval_eq_noalloc_max_scratch() bytes (256 KiB), held on every device that loads the
+ *     library until the process exits; nvars is limited to what fits (<= 26 for Goldilocks2,
+ *     <= 24 for Goldilocks3) and larger nvars (or nvars == 0) is rejected with WHIR_ERR_INVALID.
+ *   - The first call on each device looks up the array's device address (cudaGetSymbolAddress,
+ *     with that device current); make that first call before any stream capture.
+ *   - All calls share the array and it keeps the last call's tables; every call rewrites the
+ *     tables before reading them. Calls whose work overlaps on the GPU (different streams, or
+ *     different host threads on the same device) race on the array: serialise them.
+ * Errors are reported through whir_noalloc_last_error(). */
+int whir_eval_eq_noalloc(int field, uint64_t* acc_dev, const uint64_t* point_dev, size_t nvars,
+                         const uint64_t* scalar, void* stream);
+size_t whir_eval_eq_noalloc_max_scratch(void);
+const char* whir_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

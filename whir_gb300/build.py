@@ -11,7 +11,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libwhir_gb300.so")
-SOURCES = ["commit.cu", "sumcheck.cu", "prover.cu"]
+SOURCES = ["commit.cu", "sumcheck.cu", "prover.cu", "noalloc.cu"]
 HEADERS = ["field.cuh", "hash.cuh", "kernels.hpp", "protocol.hpp", "status.hpp"]
 
 NVCC_FLAGS = [

@@ -1,0 +1,98 @@
+// eval_eq for callers that cannot allocate device memory.
+//
+// Some callers cannot call cudaMalloc at the point where they need this operation: code running
+// inside a CUDA stream capture (allocation is not a capturable operation), host libraries that
+// embed the prover behind an allocator they do not control, or callers holding a fixed memory
+// budget. whir_eval_eq_noalloc takes only caller-owned device buffers and keeps its one piece of
+// scratch (the two eq tables) in a file-scope device array, so it performs no allocation at all.
+//
+// The scratch array lives for as long as the library is loaded, on every device that loads it.
+// Host code cannot use the array's name as a device address (in host code the symbol is only a
+// host-side stand-in), so the device address is looked up once per device with
+// cudaGetSymbolAddress, with that device current, during the first call made on that device.
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+
+#include "../../include/whir_gb300.h"
+#include "field.cuh"
+#include "kernels.hpp"
+
+namespace {
+
+// Room for the hi and lo eq tables: 2^ceil(nvars/2) + 2^floor(nvars/2) elements.
+constexpr size_t NOALLOC_SCRATCH_BYTES = 256 * 1024;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+constexpr int MAX_DEVICES = 64;
+std::mutex g_mu;
+void* g_scratch_ptr[MAX_DEVICES] = {nullptr};
+thread_local std::string g_err;
+
+int fail(int code, const std::string& m) {
+  g_err = m;
+  return code;
+}
+
+// Device address of the scratch array on the current device (looked up once per device).
+int scratch_address(int device, void** out) {
+  std::lock_guard<std::mutex> g(g_mu);
+  if (!g_scratch_ptr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return fail(WHIR_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    g_scratch_ptr[device] = p;
+  }
+  *out = g_scratch_ptr[device];
+  return 0;
+}
+
+template <class T>
+int run(uint64_t* acc, const uint64_t* point, size_t nvars, const uint64_t* scalar, cudaStream_t stream,
+        void* scratch) {
+  const size_t h = nvars / 2, l = nvars - h;
+  const size_t need = ((size_t(1) << h) + (size_t(1) << l)) * sizeof(T);
+  if (need > NOALLOC_SCRATCH_BYTES)
+    return fail(WHIR_ERR_INVALID, "nvars too large for the no-allocation scratch (" + std::to_string(need) +
+                                      " bytes needed, " + std::to_string(NOALLOC_SCRATCH_BYTES) + " available)");
+  T s;
+  for (int d = 0; d < T::LIMBS; ++d) {
+    if (scalar[d] >= whir::GL_P) return fail(WHIR_ERR_INVALID, "non-canonical scalar");
+    reinterpret_cast<uint64_t*>(&s)[d] = scalar[d];
+  }
+  cudaError_t e = whir::launch_eval_eq<T>(reinterpret_cast<T*>(acc), reinterpret_cast<const T*>(point), (int)nvars,
+                                          s, reinterpret_cast<T*>(scratch), stream);
+  if (e != cudaSuccess) return fail(WHIR_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* whir_noalloc_last_error(void) { return g_err.c_str(); }
+
+size_t whir_eval_eq_noalloc_max_scratch(void) { return NOALLOC_SCRATCH_BYTES; }
+
+int whir_eval_eq_noalloc(int field, uint64_t* acc_dev, const uint64_t* point_dev, size_t nvars,
+                         const uint64_t* scalar, void* stream) {
+  if (!acc_dev || !scalar || (nvars > 0 && !point_dev)) return fail(WHIR_ERR_INVALID, "null argument");
+  if (nvars == 0 || nvars > 62) return fail(WHIR_ERR_INVALID, "nvars must be in [1, 62]");
+  int device = -1;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e != cudaSuccess) return fail(WHIR_ERR_NO_DEVICE, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  if (device < 0 || device >= MAX_DEVICES) return fail(WHIR_ERR_INVALID, "device index out of range");
+  void* scratch = nullptr;
+  int rc = scratch_address(device, &scratch);
+  if (rc) return rc;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  switch (field) {
+    case WHIR_GOLDILOCKS1: return run<whir::Gl>(acc_dev, point_dev, nvars, scalar, s, scratch);
+    case WHIR_GOLDILOCKS2: return run<whir::Gl2>(acc_dev, point_dev, nvars, scalar, s, scratch);
+    case WHIR_GOLDILOCKS3: return run<whir::Gl3>(acc_dev, point_dev, nvars, scalar, s, scratch);
+    default: return fail(WHIR_ERR_INVALID, "unsupported field id");
+  }
+}
+
+}  // extern "C"
