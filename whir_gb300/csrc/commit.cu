@@ -33,34 +33,68 @@ static constexpr size_t ENC_SMEM_BUDGET = 64 * 1024;  // data bytes per CTA
 static constexpr int ENC_MAX_LOGN_SMEM = 12;          // largest in-CTA NTT
 
 
+// LOGR consecutive decimation-in-frequency stages done in registers. The current sub-blocks have
+// size B = 2^logB; a work item (vector v, sub-block blk, offset j < B/R) owns the R = 2^LOGR
+// elements at offsets j + k*B/R, k < R, which are exactly the elements those stages combine.
+// Stage st pairs k with k + R/2^(st+1) and multiplies the difference by w_(2h)^(offset mod 2h),
+// 2h = B / 2^st, read from tw[q] = w_n^q.
+template <class F, int LOGR>
+__device__ __forceinline__ void dif_step(F* s, int logn, int logB, int nvec, int lognvec, int vs, int es,
+                                         bool vec_fastest, const Gl* tw) {
+  constexpr int R = 1 << LOGR;
+  const int logstride = logB - LOGR;
+  const int stride = 1 << logstride;
+  const int items_log = logn - LOGR;  // work items per vector = n / R
+  const int total = nvec << items_log;
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    int v, it;
+    if (vec_fastest) {
+      v = t & (nvec - 1);
+      it = t >> lognvec;
+    } else {
+      v = t >> items_log;
+      it = t & ((1 << items_log) - 1);
+    }
+    const int blk = it >> logstride, j = it & (stride - 1);
+    F* base = s + v * vs + (((blk << logB) + j) * es);
+    const int kstep = stride * es;
+    F x[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) x[k] = base[k * kstep];
+#pragma unroll
+    for (int st = 0; st < LOGR; ++st) {
+      const int half = R >> (st + 1);
+      const int log2h = logB - st;
+      const int tws = logn - log2h;
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        if (k & half) continue;
+        const int pos = (j + k * stride) & ((1 << log2h) - 1);
+        const F u = x[k], w = x[k + half];
+        x[k] = u + w;
+        x[k + half] = (u - w).mul_base(tw[pos << tws]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) base[k * kstep] = x[k];
+  }
+  __syncthreads();
+}
+
 // In-place DIF NTT of nvec vectors of size 2^logn in shared memory; element i of vector v lives at
-// s[v*vs + i*es]. Output index k ends up at position brev(k).
+// s[v*vs + i*es]. Output index k ends up at position brev(k). Stages are processed three at a time
+// in registers (radix 8), with a radix-4 / radix-2 step for the remainder.
 template <class F>
 __device__ void smem_ntt_dif(F* s, int logn, int nvec, int vs, int es, bool vec_fastest, const Gl* tw) {
-  const int half = (1 << logn) >> 1;
-  const int total = nvec * half;
-  for (int st = logn - 1; st >= 0; --st) {
-    const int h = 1 << st;
-    const int tws = logn - 1 - st;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-      int v, b;
-      if (vec_fastest) {
-        v = t & (nvec - 1);
-        b = t / nvec;
-      } else {
-        v = t >> (logn - 1);
-        b = t & (half - 1);
-      }
-      const int j = b & (h - 1);
-      const int i0 = ((b >> st) << (st + 1)) + j;
-      F* p0 = s + v * vs + i0 * es;
-      F* p1 = p0 + h * es;
-      F u = *p0, w = *p1;
-      *p0 = u + w;
-      *p1 = (u - w).mul_base(tw[j << tws]);
-    }
-    __syncthreads();
+  int lognvec = 0;
+  while ((1 << lognvec) < nvec) ++lognvec;
+  int logB = logn;
+  while (logB >= 3) {
+    dif_step<F, 3>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
+    logB -= 3;
   }
+  if (logB == 2) dif_step<F, 2>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
+  if (logB == 1) dif_step<F, 1>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
 }
 
 template <class F>
@@ -168,16 +202,42 @@ __global__ void __launch_bounds__(ENC_THREADS) encode_rows_kernel(EncArgs<F> a) 
       row = c_base * C + k1 + ((uint64_t)rho << a.logC1);
       base = brev(rho, logn);
     }
-    WordHasher<KIND> h;
-    h.init((uint32_t)(M * F::LIMBS * 8));
-    for (int m = 0; m < M; ++m) {
-      uint32_t w[2 * F::LIMBS];
-      push_elem_words<F>(s[base + (m << logn)], w);
-#pragma unroll
-      for (int q = 0; q < 2 * F::LIMBS; ++q) h.push(w[q]);
-    }
     uint32_t out[8];
-    h.finish(out);
+    if constexpr (KIND == HASH_BLAKE3) {
+      // Message blocks assembled in registers (static indices) straight from shared memory:
+      // block b holds u64 limbs 8b .. 8b+7 of the row (limb L = limb L % LIMBS of column L / LIMBS).
+      const int limbs = M * F::LIMBS;
+      const int nblocks = limbs == 0 ? 1 : (limbs + 7) / 8;
+      blake3_iv(out);
+      for (int b = 0; b < nblocks; ++b) {
+        uint32_t mw[16];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int L = b * 8 + q;
+          uint64_t limb = 0;
+          if (L < limbs) {
+            const int col = L / F::LIMBS, part = L - col * F::LIMBS;
+            limb = reinterpret_cast<const uint64_t*>(&s[base + (col << logn)])[part];
+          }
+          mw[2 * q] = (uint32_t)limb;
+          mw[2 * q + 1] = (uint32_t)(limb >> 32);
+        }
+        const bool last = b == nblocks - 1;
+        const uint32_t blen = last ? (uint32_t)(limbs - b * 8) * 8 : 64;
+        const uint32_t flags = (b == 0 ? B3_CHUNK_START : 0) | (last ? (B3_CHUNK_END | B3_ROOT) : 0);
+        blake3_compress_cv(out, mw, 0, 0, blen, flags);
+      }
+    } else {
+      WordHasher<KIND> h;
+      h.init((uint32_t)(M * F::LIMBS * 8));
+      for (int m = 0; m < M; ++m) {
+        uint32_t w[2 * F::LIMBS];
+        push_elem_words<F>(s[base + (m << logn)], w);
+#pragma unroll
+        for (int q = 0; q < 2 * F::LIMBS; ++q) h.push(w[q]);
+      }
+      h.finish(out);
+    }
     uint4* dstw = reinterpret_cast<uint4*>(a.leaves + row * 8);
     dstw[0] = make_uint4(out[0], out[1], out[2], out[3]);
     dstw[1] = make_uint4(out[4], out[5], out[6], out[7]);
@@ -464,23 +524,48 @@ struct PowArgs {
   uint32_t chal[8];
   uint64_t threshold, start, count;
   unsigned long long* best;
+  unsigned long long* counter;
 };
 
+static constexpr int POW_THREADS = 256;
+static constexpr int POW_PER_THREAD = 4;
+static constexpr uint64_t POW_BLOCK = (uint64_t)POW_THREADS * POW_PER_THREAD;
+
+// CTAs claim consecutive blocks of POW_BLOCK nonces in increasing order and stop at the first block
+// that starts at or above the best nonce found so far. Every block below the final best has been
+// searched completely, so the result is the lowest satisfying nonce of the range.
 template <int KIND>
-__global__ void __launch_bounds__(256) pow_kernel(PowArgs a) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < a.count; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t nonce = a.start + i;
-    uint32_t m[16];
+__global__ void __launch_bounds__(POW_THREADS) pow_kernel(PowArgs a) {
+  __shared__ unsigned long long s_start;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const unsigned long long b = atomicAdd(a.counter, 1ull);
+      const unsigned long long off = b * POW_BLOCK;
+      const unsigned long long st = a.start + off;
+      const unsigned long long best = *reinterpret_cast<volatile unsigned long long*>(a.best);
+      s_start = (off >= a.count || st >= best) ? ~0ull : st;
+    }
+    __syncthreads();
+    const unsigned long long st = s_start;
+    __syncthreads();
+    if (st == ~0ull) return;
+#pragma unroll 1
+    for (int q = 0; q < POW_PER_THREAD; ++q) {
+      const uint64_t off = (uint64_t)q * POW_THREADS + threadIdx.x;
+      if (st - a.start + off >= a.count) break;
+      const uint64_t nonce = st + off;
+      uint32_t m[16];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) m[q] = a.chal[q];
-    m[8] = (uint32_t)nonce;
-    m[9] = (uint32_t)(nonce >> 32);
+      for (int w = 0; w < 8; ++w) m[w] = a.chal[w];
+      m[8] = (uint32_t)nonce;
+      m[9] = (uint32_t)(nonce >> 32);
 #pragma unroll
-    for (int q = 10; q < 16; ++q) m[q] = 0;
-    uint32_t h[8];
-    hash64<KIND>(m, h);
-    const uint64_t v = (uint64_t)h[0] | ((uint64_t)h[1] << 32);
-    if (v <= a.threshold) atomicMin(a.best, (unsigned long long)nonce);
+      for (int w = 10; w < 16; ++w) m[w] = 0;
+      uint32_t h[8];
+      hash64<KIND>(m, h);
+      const uint64_t v = (uint64_t)h[0] | ((uint64_t)h[1] << 32);
+      if (v <= a.threshold) atomicMin(a.best, (unsigned long long)nonce);
+    }
   }
 }
 
@@ -492,7 +577,8 @@ cudaError_t launch_pow(const uint32_t challenge[8], uint64_t threshold, uint64_t
   a.start = start;
   a.count = count;
   a.best = best;
-  unsigned grid = (unsigned)std::min<uint64_t>((count + 255) / 256, 152ull * 16);
+  a.counter = best + 1;  // the caller provides two words: best nonce, block counter (both reset)
+  unsigned grid = (unsigned)std::min<uint64_t>((count + POW_BLOCK - 1) / POW_BLOCK, 152ull * 8);
   switch (kind) {
     case HASH_BLAKE3: pow_kernel<HASH_BLAKE3><<<grid, 256, 0, s>>>(a); note_launch(); break;
     case HASH_SHA2: pow_kernel<HASH_SHA2><<<grid, 256, 0, s>>>(a); note_launch(); break;

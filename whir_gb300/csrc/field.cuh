@@ -23,15 +23,119 @@ namespace whir {
 static constexpr uint64_t GL_P = 0xFFFFFFFF00000001ULL;
 static constexpr uint64_t GL_EPS = 0xFFFFFFFFULL;
 
+#if defined(__CUDA_ARCH__)
+// Device versions on 32-bit halves with PTX carry chains (fewer compare/select instructions on the
+// ALU pipe than the 64-bit C expressions). Same canonical inputs and outputs as the host versions.
+__device__ __forceinline__ uint64_t gl_add_ptx(uint64_t a, uint64_t b) {
+  uint64_t r;
+  // s = a + b (carry c); t = s + eps (carry c2). The canonical sum is t when c | c2, else s.
+  asm("{\n\t"
+      ".reg .u32 a0, a1, b0, b1, s0, s1, t0, t1, c, c2;\n\t"
+      ".reg .pred p;\n\t"
+      "mov.b64 {a0, a1}, %1;\n\t"
+      "mov.b64 {b0, b1}, %2;\n\t"
+      "add.cc.u32 s0, a0, b0;\n\t"
+      "addc.cc.u32 s1, a1, b1;\n\t"
+      "addc.u32 c, 0, 0;\n\t"
+      "add.cc.u32 t0, s0, 0xffffffff;\n\t"
+      "addc.cc.u32 t1, s1, 0;\n\t"
+      "addc.u32 c2, 0, 0;\n\t"
+      "or.b32 c, c, c2;\n\t"
+      "setp.ne.u32 p, c, 0;\n\t"
+      "selp.b32 s0, t0, s0, p;\n\t"
+      "selp.b32 s1, t1, s1, p;\n\t"
+      "mov.b64 %0, {s0, s1};\n\t"
+      "}"
+      : "=l"(r)
+      : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t gl_sub_ptx(uint64_t a, uint64_t b) {
+  uint64_t r;
+  // d = a - b; on borrow subtract eps as well (adding p modulo 2^64).
+  asm("{\n\t"
+      ".reg .u32 a0, a1, b0, b1, d0, d1, bw;\n\t"
+      "mov.b64 {a0, a1}, %1;\n\t"
+      "mov.b64 {b0, b1}, %2;\n\t"
+      "sub.cc.u32 d0, a0, b0;\n\t"
+      "subc.cc.u32 d1, a1, b1;\n\t"
+      "subc.u32 bw, 0, 0;\n\t"
+      "sub.cc.u32 d0, d0, bw;\n\t"
+      "subc.u32 d1, d1, 0;\n\t"
+      "mov.b64 %0, {d0, d1};\n\t"
+      "}"
+      : "=l"(r)
+      : "l"(a), "l"(b));
+  return r;
+}
+// 64x64 -> 128 product in four 32-bit limbs r3:r2:r1:r0, then
+//   x = (r1:r0) + r2 * 2^64 + r3 * 2^96 = (r1:r0) - r3 + r2 * (2^32 - 1)   (mod p)
+// with each borrow / carry folded back as -eps / +eps, and a final conditional subtraction of p.
+__device__ __forceinline__ uint64_t gl_mul_ptx(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("{\n\t"
+      ".reg .u32 a0, a1, b0, b1, r0, r1, r2, r3, bw, y0, y1, c, t0, t1, z;\n\t"
+      ".reg .pred p;\n\t"
+      "mov.b64 {a0, a1}, %1;\n\t"
+      "mov.b64 {b0, b1}, %2;\n\t"
+      "mov.u32 z, 0;\n\t"
+      "mul.lo.u32 r0, a0, b0;\n\t"
+      "mul.hi.u32 r1, a0, b0;\n\t"
+      "mad.lo.cc.u32 r1, a0, b1, r1;\n\t"
+      "madc.hi.u32 r2, a0, b1, z;\n\t"
+      "mad.lo.cc.u32 r1, a1, b0, r1;\n\t"
+      "madc.hi.cc.u32 r2, a1, b0, r2;\n\t"
+      "addc.u32 r3, z, z;\n\t"
+      "mad.lo.cc.u32 r2, a1, b1, r2;\n\t"
+      "madc.hi.u32 r3, a1, b1, r3;\n\t"
+      // w = (r1:r0) - r3, minus eps on borrow
+      "sub.cc.u32 r0, r0, r3;\n\t"
+      "subc.cc.u32 r1, r1, z;\n\t"
+      "subc.u32 bw, z, z;\n\t"
+      "sub.cc.u32 r0, r0, bw;\n\t"
+      "subc.u32 r1, r1, z;\n\t"
+      // y = r2 * (2^32 - 1) = (r2 << 32) - r2
+      "sub.cc.u32 y0, z, r2;\n\t"
+      "subc.u32 y1, r2, z;\n\t"
+      // w += y, plus eps on carry
+      "add.cc.u32 r0, r0, y0;\n\t"
+      "addc.cc.u32 r1, r1, y1;\n\t"
+      "addc.u32 c, z, z;\n\t"
+      "sub.u32 c, z, c;\n\t"
+      "add.cc.u32 r0, r0, c;\n\t"
+      "addc.u32 r1, r1, z;\n\t"
+      // canonical: if w + eps carries, w >= p and the result is w + eps mod 2^64
+      "add.cc.u32 t0, r0, 0xffffffff;\n\t"
+      "addc.cc.u32 t1, r1, z;\n\t"
+      "addc.u32 c, z, z;\n\t"
+      "setp.ne.u32 p, c, 0;\n\t"
+      "selp.b32 r0, t0, r0, p;\n\t"
+      "selp.b32 r1, t1, r1, p;\n\t"
+      "mov.b64 %0, {r0, r1};\n\t"
+      "}"
+      : "=l"(r)
+      : "l"(a), "l"(b));
+  return r;
+}
+#endif
+
 WHIR_HD uint64_t gl_add(uint64_t a, uint64_t b) {
+#if defined(__CUDA_ARCH__)
+  return gl_add_ptx(a, b);
+#else
   uint64_t s = a + b;
   uint64_t w = (s < a) ? GL_EPS : 0;  // wrapped past 2^64: add 2^64 mod p
   s += w;
   return (s >= GL_P) ? s - GL_P : s;
+#endif
 }
 WHIR_HD uint64_t gl_sub(uint64_t a, uint64_t b) {
+#if defined(__CUDA_ARCH__)
+  return gl_sub_ptx(a, b);
+#else
   uint64_t d = a - b;
   return (a < b) ? d - GL_EPS : d;
+#endif
 }
 WHIR_HD uint64_t gl_neg(uint64_t a) { return a ? GL_P - a : 0; }
 
@@ -47,7 +151,7 @@ WHIR_HD uint64_t gl_reduce(uint64_t lo, uint64_t hi) {
 
 WHIR_HD uint64_t gl_mul(uint64_t a, uint64_t b) {
 #if defined(__CUDA_ARCH__)
-  return gl_reduce(a * b, __umul64hi(a, b));
+  return gl_mul_ptx(a, b);
 #else
   unsigned __int128 x = (unsigned __int128)a * b;
   return gl_reduce((uint64_t)x, (uint64_t)(x >> 64));

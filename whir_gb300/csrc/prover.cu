@@ -238,13 +238,15 @@ uint64_t grind(whir_ctx* ctx, int kind, const uint8_t chal[32], uint64_t thresho
   for (int i = 0; i < 8; ++i)
     cw[i] = (uint32_t)chal[4 * i] | ((uint32_t)chal[4 * i + 1] << 8) | ((uint32_t)chal[4 * i + 2] << 16) |
             ((uint32_t)chal[4 * i + 3] << 24);
-  // Chunk sized to the expected work: ~4x the mean number of trials, at least 2^20.
   double expect = 18446744073709551616.0 / ((double)threshold + 1.0);
-  uint64_t chunk = 1ull << 20;
-  while ((double)chunk < 4.0 * expect && chunk < (1ull << 30)) chunk <<= 1;
+  // The search kernel stops as soon as every block below the best hit is done, so the range per
+  // launch can be generous (one launch almost always suffices).
+  uint64_t chunk = 1ull << 22;
+  while ((double)chunk < 64.0 * expect && chunk < (1ull << 36)) chunk <<= 1;
   const uint64_t limit = 1ull << 50;
   for (uint64_t start = 0; start < limit; start += chunk) {
     CU(cudaMemsetAsync(ctx->d_pow, 0xff, sizeof(unsigned long long), ctx->stream));
+    CU(cudaMemsetAsync(ctx->d_pow + 1, 0, sizeof(unsigned long long), ctx->stream));
     {
       ProfScope prof(ctx, PF_POW);
       CU(launch_pow(cw, threshold, start, chunk, ctx->d_pow, kind, ctx->stream));
@@ -901,7 +903,7 @@ int whir_ctx_create(int device, whir_ctx** out) {
     CU(cudaMemcpy(ctx->d_roots, tab.data(), tab.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
     ctx->rt.lo = ctx->d_roots;
     ctx->rt.hi = ctx->d_roots + (1u << 16);
-    CU(cudaMalloc((void**)&ctx->d_pow, sizeof(unsigned long long)));
+    CU(cudaMalloc((void**)&ctx->d_pow, 2 * sizeof(unsigned long long)));
     stage_reserve(ctx.get(), 1 << 20);
     ctx->launches_at_create = kernel_launches();
     *out = ctx.release();
