@@ -67,12 +67,17 @@ cudaError_t launch_gather_digests(const uint32_t* nodes, const uint64_t* idx, si
 // Number of partial (c0, c2) pairs written by the reduce kernels for a vector of n elements.
 size_t sumcheck_partials(size_t n);
 
+// The (c0, c2) kernels below write one partial pair per block. When `counter` is non-null (a zeroed
+// u32 on the device) the last block also sums the partials into out[0..2) and re-zeroes the
+// counter, so no separate reduce launch is needed.
 // (c0, c2) of vectors a, b of n = 2^k elements -> partials (2 elements per block)
 template <class T>
-cudaError_t launch_sumcheck_compute(const T* a, const T* b, size_t n, T* partials, size_t* nparts, cudaStream_t s);
+cudaError_t launch_sumcheck_compute(const T* a, const T* b, size_t n, T* partials, size_t* nparts, cudaStream_t s,
+                                    T* out = nullptr, unsigned int* counter = nullptr);
 // Folds a, b (n elements) with weight r in place to n/2 and computes (c0, c2) of the result.
 template <class T>
-cudaError_t launch_fold_compute(T* a, T* b, size_t n, T r, T* partials, size_t* nparts, cudaStream_t s);
+cudaError_t launch_fold_compute(T* a, T* b, size_t n, T r, T* partials, size_t* nparts, cudaStream_t s,
+                                T* out = nullptr, unsigned int* counter = nullptr);
 // v[i] += (v[i + n/2] - v[i]) * r for i < n/2
 template <class T>
 cudaError_t launch_fold(T* v, size_t n, T r, cudaStream_t s);
@@ -107,11 +112,12 @@ cudaError_t launch_add(T* acc, const T* src, size_t n, cudaStream_t s);
 // h = nv/2, l = nv - h, scalar folded into hi).
 template <class T, class S>
 cudaError_t launch_first_compute_eq(const S* x, size_t n, const T* tables, int nforms, int nv, T* partials,
-                                    size_t* nparts, cudaStream_t s);
+                                    size_t* nparts, cudaStream_t s, T* out = nullptr, unsigned int* counter = nullptr);
 // Folds map(x) and the eq covector with r (n -> n/2) into a_out / b_out and computes (c0, c2).
 template <class T, class S>
 cudaError_t launch_first_fold_compute_eq(const S* x, size_t n, T r, const T* tables, int nforms, int nv, T* a_out,
-                                         T* b_out, T* partials, size_t* nparts, cudaStream_t s);
+                                         T* b_out, T* partials, size_t* nparts, cudaStream_t s, T* out = nullptr,
+                                         unsigned int* counter = nullptr);
 // Builds the eq table of `cnt` coordinates point[off..off+cnt) scaled by scalar (device arrays).
 template <class T>
 cudaError_t launch_eq_table(const T* point, int off, int cnt, T scalar, T* table, cudaStream_t s);

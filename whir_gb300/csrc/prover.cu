@@ -52,6 +52,8 @@ struct whir_ctx {
   RootTab rt{};
   uint8_t* h_stage = nullptr;  // pinned staging for small transfers
   size_t h_stage_cap = 0;
+  uint8_t* h_up = nullptr;  // pinned upload arena (see h2d)
+  size_t up_cap = 0, up_off = 0;
   unsigned long long* d_pow = nullptr;
   uint64_t launches_at_create = 0;
   uint64_t h2d_bytes = 0, d2h_bytes = 0;
@@ -166,14 +168,29 @@ void d2h(whir_ctx* ctx, void* dst, const void* src, size_t bytes) {
   stage_reserve(ctx, bytes);
   CU(cudaMemcpyAsync(ctx->h_stage, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
+  ctx->up_off = 0;  // every earlier upload has completed
   memcpy(dst, ctx->h_stage, bytes);
 }
 // Host -> device copy of a small argument (stream ordered; host buffer reusable on return).
+// Host -> device copy of a small argument without waiting: the bytes are staged in a pinned upload
+// arena whose space is recycled only after the stream has been synchronised (every d2h() does).
 void h2d(whir_ctx* ctx, void* dst, const void* src, size_t bytes) {
   if (!bytes) return;
   ctx->h2d_bytes += bytes;
-  CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
-  CU(cudaStreamSynchronize(ctx->stream));
+  if (bytes > ctx->up_cap) {
+    CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    ctx->up_off = 0;
+    return;
+  }
+  if (ctx->up_off + bytes > ctx->up_cap) {
+    CU(cudaStreamSynchronize(ctx->stream));
+    ctx->up_off = 0;
+  }
+  uint8_t* slot = ctx->h_up + ctx->up_off;
+  memcpy(slot, src, bytes);
+  CU(cudaMemcpyAsync(dst, slot, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  ctx->up_off += (bytes + 255) & ~(size_t)255;
 }
 
 template <class T>
@@ -204,6 +221,8 @@ struct whir_witness {
   DBuf<uint64_t> matrix;  // codeword_len x num_cols elements, elem_limbs u64 each
   DBuf<uint32_t> nodes;   // (2^(layers+1) - 1) x 8 words
   uint8_t root[32] = {0};
+  const uint64_t* host_src = nullptr;  // host buffer the committed vectors were copied from
+  DBuf<uint64_t> vectors;              // device copy of those vectors (commit from host memory)
   std::vector<uint64_t> ood_points;  // target limbs
   std::vector<uint64_t> ood_matrix;  // points x vectors, target limbs
   size_t num_vectors(size_t t_limbs) const {
@@ -404,7 +423,11 @@ void irs_open(whir_ctx* ctx, const Irs& c, Transcript& ts, const std::vector<con
 template <class T>
 struct SumcheckBuffers {
   DBuf<T> parts, out;
-  SumcheckBuffers(whir_ctx* ctx, size_t n) : parts(ctx, 2 * sumcheck_partials(n) + 2), out(ctx, 2) {}
+  DBuf<unsigned int> counter;  // last-block reduction counter (kept at zero between launches)
+  SumcheckBuffers(whir_ctx* ctx, size_t n)
+      : parts(ctx, 2 * sumcheck_partials(n) + 2), out(ctx, 2), counter(ctx, 1) {
+    CU(cudaMemsetAsync(counter.p, 0, sizeof(unsigned int), ctx->stream));
+  }
 };
 
 template <class T>
@@ -421,12 +444,11 @@ std::vector<T> sumcheck_device(whir_ctx* ctx, const Sumcheck& c, Transcript& ts,
     {
       ProfScope prof(ctx, PF_SUMCHECK);
       if (!have) {
-        CU(launch_sumcheck_compute<T>(a, b, n, buf.parts.p, &np, ctx->stream));
+        CU(launch_sumcheck_compute<T>(a, b, n, buf.parts.p, &np, ctx->stream, buf.out.p, buf.counter.p));
       } else {
-        CU(launch_fold_compute<T>(a, b, n, prev, buf.parts.p, &np, ctx->stream));
+        CU(launch_fold_compute<T>(a, b, n, prev, buf.parts.p, &np, ctx->stream, buf.out.p, buf.counter.p));
         n = n > 1 ? n / 2 : n;
       }
-      CU(launch_reduce_pairs<T>(buf.parts.p, np, buf.out.p, ctx->stream));
     }
     T cc[2];
     d2h(ctx, cc, buf.out.p, sizeof(cc));
@@ -467,16 +489,16 @@ std::vector<T> initial_sumcheck_fused(whir_ctx* ctx, const Sumcheck& c, Transcri
     {
       ProfScope prof(ctx, PF_SUMCHECK);
       if (round == 0) {
-        CU((launch_first_compute_eq<T, S>(x, n, tables, nforms, nvars, buf.parts.p, &np, ctx->stream)));
+        CU((launch_first_compute_eq<T, S>(x, n, tables, nforms, nvars, buf.parts.p, &np, ctx->stream, buf.out.p,
+                                          buf.counter.p)));
       } else if (round == 1) {
         CU((launch_first_fold_compute_eq<T, S>(x, n, prev, tables, nforms, nvars, a, b, buf.parts.p, &np,
-                                               ctx->stream)));
+                                               ctx->stream, buf.out.p, buf.counter.p)));
         n /= 2;
       } else {
-        CU(launch_fold_compute<T>(a, b, n, prev, buf.parts.p, &np, ctx->stream));
+        CU(launch_fold_compute<T>(a, b, n, prev, buf.parts.p, &np, ctx->stream, buf.out.p, buf.counter.p));
         n = n > 1 ? n / 2 : n;
       }
-      CU(launch_reduce_pairs<T>(buf.parts.p, np, buf.out.p, ctx->stream));
     }
     T cc[2];
     d2h(ctx, cc, buf.out.p, sizeof(cc));
@@ -905,6 +927,8 @@ int whir_ctx_create(int device, whir_ctx** out) {
     ctx->rt.hi = ctx->d_roots + (1u << 16);
     CU(cudaMalloc((void**)&ctx->d_pow, 2 * sizeof(unsigned long long)));
     stage_reserve(ctx.get(), 1 << 20);
+    ctx->up_cap = 8 << 20;
+    CU(cudaMallocHost((void**)&ctx->h_up, ctx->up_cap));
     ctx->launches_at_create = kernel_launches();
     *out = ctx.release();
     return 0;
@@ -923,6 +947,7 @@ int whir_ctx_destroy(whir_ctx* ctx) {
   if (ctx->d_roots) cudaFree(ctx->d_roots);
   if (ctx->d_pow) cudaFree(ctx->d_pow);
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+  if (ctx->h_up) cudaFreeHost(ctx->h_up);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return 0;
@@ -1113,10 +1138,22 @@ int whir_commit(whir_ctx* ctx, const whir_config* cfg, whir_prover_state* ps, co
     if (!cfg || !ps || !vectors || !out) throw Error(WHIR_ERR_INVALID, "null argument");
     const Config& c = cfg->cfg;
     return with_embedding(c.field, [&]<class S, class T>() {
-      DBuf<S> holder;
-      const S* d = device_vectors<S>(ctx, vectors, c.initial.num_vectors * c.size(), flags, holder, false);
+      const size_t count = c.initial.num_vectors * c.size();
+      DBuf<uint64_t> copy;
+      const S* d = reinterpret_cast<const S*>(vectors);
+      if (!(flags & WHIR_DEVICE_PTRS)) {
+        copy = DBuf<uint64_t>(ctx, count * S::LIMBS);
+        ctx->h2d_bytes += count * sizeof(S);
+        CU(cudaMemcpyAsync(copy.p, vectors, count * sizeof(S), cudaMemcpyHostToDevice, ctx->stream));
+        d = reinterpret_cast<const S*>(copy.p);
+      }
       auto w = irs_commit<S, T>(ctx, c.initial, ps->ts, d, c.field);
       CU(cudaStreamSynchronize(ctx->stream));
+      if (!(flags & WHIR_DEVICE_PTRS)) {
+        // Keep the device copy: prove() given the same host buffer reuses it instead of copying again.
+        w->host_src = vectors;
+        w->vectors = std::move(copy);
+      }
       *out = w.release();
       return 0;
     });
@@ -1159,7 +1196,12 @@ int whir_prove(whir_ctx* ctx, const whir_config* cfg, whir_prover_state* ps, con
       for (size_t i = 0; i < n_covectors; ++i) covs.push_back(load_host<T>(covectors + i * n * T::LIMBS, n));
       std::vector<T> evals = nforms * nv ? load_host<T>(evaluations, nforms * nv) : std::vector<T>();
       DBuf<S> holder;
-      const S* d = nv ? device_vectors<S>(ctx, vectors, nv * n, flags, holder, false) : nullptr;
+      const S* d = nullptr;
+      if (nv && !(flags & WHIR_DEVICE_PTRS) && ws.size() == 1 && ws[0]->host_src == vectors && ws[0]->vectors.p) {
+        d = reinterpret_cast<const S*>(ws[0]->vectors.p);  // same host buffer as the commitment
+      } else if (nv) {
+        d = device_vectors<S>(ctx, vectors, nv * n, flags, holder, false);
+      }
       std::vector<T> ep, rlc;
       prove_device<S, T>(ctx, c, ps->ts, d, nv, ws, pts, covs, evals, ep, rlc);
       if (eval_point_out) store_host<T>(ep, eval_point_out);

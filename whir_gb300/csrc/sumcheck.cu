@@ -52,13 +52,55 @@ __device__ T block_sum(T x) {
   return x;
 }
 
+template <class T>
+__device__ __forceinline__ T ldcg_t(const T* p) {
+  T r;
+  const unsigned long long* s = reinterpret_cast<const unsigned long long*>(p);
+  unsigned long long* d = reinterpret_cast<unsigned long long*>(&r);
+#pragma unroll
+  for (int i = 0; i < (int)(sizeof(T) / 8); ++i) d[i] = __ldcg(s + i);
+  return r;
+}
+
+// Stores this block's (c0, c2) partial. With a counter, the last block to finish also sums all
+// partials into out[0..2) and re-arms the counter, so one launch yields the round message.
+template <class T>
+__device__ void finish_pairs(T acc0, T acc2, T* partials, T* out, unsigned int* counter) {
+  __shared__ bool am_last;
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = acc0;
+    partials[2 * blockIdx.x + 1] = acc2;
+    am_last = false;
+    if (counter) {
+      __threadfence();
+      am_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+  }
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  T s0 = T::zero(), s2 = T::zero();
+  for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
+    s0 += ldcg_t(partials + 2 * i);
+    s2 += ldcg_t(partials + 2 * i + 1);
+  }
+  s0 = block_sum(s0);
+  s2 = block_sum(s2);
+  if (threadIdx.x == 0) {
+    out[0] = s0;
+    out[1] = s2;
+    *counter = 0;
+  }
+}
+
 size_t sumcheck_partials(size_t n) {
   size_t work = std::max<size_t>(n / 4, 1);
   return std::min(SC_MAX_BLOCKS, (work + SC_THREADS - 1) / SC_THREADS);
 }
 
 template <class T>
-__global__ void __launch_bounds__(SC_THREADS) sc_compute_kernel(const T* a, const T* b, uint64_t n, T* partials) {
+__global__ void __launch_bounds__(SC_THREADS) sc_compute_kernel(const T* a, const T* b, uint64_t n, T* partials,
+                                                                 T* out, unsigned int* counter) {
   T acc0 = T::zero(), acc2 = T::zero();
   if (n == 1) {
     if (blockIdx.x == 0 && threadIdx.x == 0) acc0 = a[0] * b[0];
@@ -72,14 +114,12 @@ __global__ void __launch_bounds__(SC_THREADS) sc_compute_kernel(const T* a, cons
   }
   acc0 = block_sum(acc0);
   acc2 = block_sum(acc2);
-  if (threadIdx.x == 0) {
-    partials[2 * blockIdx.x] = acc0;
-    partials[2 * blockIdx.x + 1] = acc2;
-  }
+  finish_pairs(acc0, acc2, partials, out, counter);
 }
 
 template <class T>
-__global__ void __launch_bounds__(SC_THREADS) sc_fold_compute_kernel(T* a, T* b, uint64_t n, T r, T* partials) {
+__global__ void __launch_bounds__(SC_THREADS) sc_fold_compute_kernel(T* a, T* b, uint64_t n, T r, T* partials,
+                                                                      T* out, unsigned int* counter) {
   T acc0 = T::zero(), acc2 = T::zero();
   if (n <= 2) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -109,10 +149,7 @@ __global__ void __launch_bounds__(SC_THREADS) sc_fold_compute_kernel(T* a, T* b,
   }
   acc0 = block_sum(acc0);
   acc2 = block_sum(acc2);
-  if (threadIdx.x == 0) {
-    partials[2 * blockIdx.x] = acc0;
-    partials[2 * blockIdx.x + 1] = acc2;
-  }
+  finish_pairs(acc0, acc2, partials, out, counter);
 }
 
 template <class T>
@@ -148,17 +185,19 @@ __global__ void __launch_bounds__(SC_THREADS) reduce_singles_kernel(const T* par
 }
 
 template <class T>
-cudaError_t launch_sumcheck_compute(const T* a, const T* b, size_t n, T* partials, size_t* nparts, cudaStream_t s) {
+cudaError_t launch_sumcheck_compute(const T* a, const T* b, size_t n, T* partials, size_t* nparts, cudaStream_t s,
+                                    T* out, unsigned int* counter) {
   size_t g = sumcheck_partials(n);
-  sc_compute_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(a, b, n, partials);
+  sc_compute_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(a, b, n, partials, out, counter);
   note_launch();
   *nparts = g;
   return cudaGetLastError();
 }
 template <class T>
-cudaError_t launch_fold_compute(T* a, T* b, size_t n, T r, T* partials, size_t* nparts, cudaStream_t s) {
+cudaError_t launch_fold_compute(T* a, T* b, size_t n, T r, T* partials, size_t* nparts, cudaStream_t s, T* out,
+                                unsigned int* counter) {
   size_t g = sumcheck_partials(n);
-  sc_fold_compute_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(a, b, n, r, partials);
+  sc_fold_compute_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(a, b, n, r, partials, out, counter);
   note_launch();
   *nparts = g;
   return cudaGetLastError();
@@ -398,7 +437,8 @@ __device__ __forceinline__ T eq_on_the_fly(const T* tables, int nforms, int h, i
 
 template <class T, class S>
 __global__ void __launch_bounds__(SC_THREADS) first_compute_eq_kernel(const S* x, uint64_t n, const T* tables,
-                                                                      int nforms, int h, int l, T* partials) {
+                                                                      int nforms, int h, int l, T* partials,
+                                                                      T* out, unsigned int* counter) {
   T acc0 = T::zero(), acc2 = T::zero();
   const uint64_t half = n >> 1;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < half; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -409,16 +449,14 @@ __global__ void __launch_bounds__(SC_THREADS) first_compute_eq_kernel(const S* x
   }
   acc0 = block_sum(acc0);
   acc2 = block_sum(acc2);
-  if (threadIdx.x == 0) {
-    partials[2 * blockIdx.x] = acc0;
-    partials[2 * blockIdx.x + 1] = acc2;
-  }
+  finish_pairs(acc0, acc2, partials, out, counter);
 }
 
 template <class T, class S>
 __global__ void __launch_bounds__(SC_THREADS) first_fold_compute_eq_kernel(const S* x, uint64_t n, T r,
                                                                            const T* tables, int nforms, int h, int l,
-                                                                           T* a_out, T* b_out, T* partials) {
+                                                                           T* a_out, T* b_out, T* partials, T* out,
+                                                                           unsigned int* counter) {
   T acc0 = T::zero(), acc2 = T::zero();
   const uint64_t q = n >> 2, hf = n >> 1;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < q; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -437,28 +475,27 @@ __global__ void __launch_bounds__(SC_THREADS) first_fold_compute_eq_kernel(const
   }
   acc0 = block_sum(acc0);
   acc2 = block_sum(acc2);
-  if (threadIdx.x == 0) {
-    partials[2 * blockIdx.x] = acc0;
-    partials[2 * blockIdx.x + 1] = acc2;
-  }
+  finish_pairs(acc0, acc2, partials, out, counter);
 }
 
 template <class T, class S>
 cudaError_t launch_first_compute_eq(const S* x, size_t n, const T* tables, int nforms, int nv, T* partials,
-                                    size_t* nparts, cudaStream_t s) {
+                                    size_t* nparts, cudaStream_t s, T* out, unsigned int* counter) {
   size_t g = sumcheck_partials(n);
   first_compute_eq_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(x, n, tables, nforms, nv / 2, nv - nv / 2,
-                                                                    partials);
+                                                                    partials, out, counter);
   note_launch();
   *nparts = g;
   return cudaGetLastError();
 }
 template <class T, class S>
 cudaError_t launch_first_fold_compute_eq(const S* x, size_t n, T r, const T* tables, int nforms, int nv, T* a_out,
-                                         T* b_out, T* partials, size_t* nparts, cudaStream_t s) {
+                                         T* b_out, T* partials, size_t* nparts, cudaStream_t s, T* out,
+                                         unsigned int* counter) {
   size_t g = sumcheck_partials(n);
   first_fold_compute_eq_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(x, n, r, tables, nforms, nv / 2,
-                                                                         nv - nv / 2, a_out, b_out, partials);
+                                                                         nv - nv / 2, a_out, b_out, partials, out,
+                                                                         counter);
   note_launch();
   *nparts = g;
   return cudaGetLastError();
@@ -524,8 +561,9 @@ cudaError_t launch_univariate_eval(const S* coeffs, size_t n, T x, T* partials, 
 // Explicit instantiations
 // ---------------------------------------------------------------------------------------------
 #define WHIR_SC_INST(T)                                                                                  \
-  template cudaError_t launch_sumcheck_compute<T>(const T*, const T*, size_t, T*, size_t*, cudaStream_t); \
-  template cudaError_t launch_fold_compute<T>(T*, T*, size_t, T, T*, size_t*, cudaStream_t);             \
+  template cudaError_t launch_sumcheck_compute<T>(const T*, const T*, size_t, T*, size_t*, cudaStream_t, T*,      \
+                                                  unsigned int*);                                                \
+  template cudaError_t launch_fold_compute<T>(T*, T*, size_t, T, T*, size_t*, cudaStream_t, T*, unsigned int*);  \
   template cudaError_t launch_fold<T>(T*, size_t, T, cudaStream_t);                                       \
   template cudaError_t launch_reduce_pairs<T>(const T*, size_t, T*, cudaStream_t);                        \
   template cudaError_t launch_reduce_singles<T>(const T*, size_t, T*, cudaStream_t);                      \
@@ -537,9 +575,9 @@ cudaError_t launch_univariate_eval(const S* coeffs, size_t n, T x, T* partials, 
   template cudaError_t launch_add<T>(T*, const T*, size_t, cudaStream_t);                                        \
   template cudaError_t launch_eq_table<T>(const T*, int, int, T, T*, cudaStream_t);                              \
   template cudaError_t launch_first_compute_eq<T, Gl>(const Gl*, size_t, const T*, int, int, T*, size_t*,        \
-                                                      cudaStream_t);                                             \
+                                                      cudaStream_t, T*, unsigned int*);                          \
   template cudaError_t launch_first_fold_compute_eq<T, Gl>(const Gl*, size_t, T, const T*, int, int, T*, T*, T*, \
-                                                           size_t*, cudaStream_t);
+                                                           size_t*, cudaStream_t, T*, unsigned int*);
 
 WHIR_SC_INST(Gl)
 WHIR_SC_INST(Gl2)
