@@ -33,9 +33,11 @@ sys.path.insert(0, ROOT)
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 
-# DRAM bytes per launch of the dominant kernel from an ncu capture (profiles/ summaries), keyed by
-# family; None until captured.
-NCU_TRAFFIC_PER_CALL = {}
+# DRAM traffic / algorithmic bytes of a kernel family, from one ncu capture (profiles/
+# ncu_encode_and_first_sumcheck_d24.md): the initial commitment's encode_cols + encode_rows moved
+# 352.5 + 549.0 MB of DRAM for 402,653,184 algorithmic bytes. The encode kernels' traffic grows in
+# proportion to the elements they process, so per-launch traffic = algorithmic bytes x this ratio.
+NCU_TRAFFIC_RATIO = {"encode": (352.507648e6 + 548.952832e6) / 402653184.0}
 
 
 def parse_args():
@@ -329,13 +331,14 @@ def run_gpu(args):
     if fam in alg:
         per_call_bytes = alg[fam] * args.steps / calls_f
         achieved = per_call_bytes / (ms_f / calls_f * 1e-3) / 1e9
+        ratio = NCU_TRAFFIC_RATIO.get(fam)
         roofline = {"bound": "hbm", "kernel_family": fam, "achieved": achieved, "peak": peak, "unit": "GB/s",
                     "frac": achieved / peak, "peak_source": peak_kind,
-                    "traffic": NCU_TRAFFIC_PER_CALL.get(fam), "algorithmic_bytes_per_launch": per_call_bytes,
-                    "avg_launch_ms": ms_f / calls_f}
+                    "traffic": per_call_bytes * ratio if ratio else None,
+                    "algorithmic_bytes_per_launch": per_call_bytes, "avg_launch_ms": ms_f / calls_f}
     else:
         roofline = {"bound": "integer", "kernel_family": fam, "achieved": None, "peak": peak, "unit": "GB/s",
-                    "frac": None, "traffic": NCU_TRAFFIC_PER_CALL.get(fam), "avg_launch_ms": ms_f / calls_f}
+                    "frac": None, "traffic": None, "avg_launch_ms": ms_f / calls_f}
     cpu = None if args.no_cpu_baseline else cpu_baseline(args, params, vec, point)
     line = {
         "metric": "prove_ms_d%d_goldilocks2_blake3" % nv, "value": ms_per_proof_job, "unit": "ms",
