@@ -50,6 +50,10 @@ def parse_args():
     ap.add_argument("--cpu-nv", type=int, default=20, help="size of the bounded CPU-baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched / serving measurements")
+    ap.add_argument("--batch-jobs", type=int, default=64)
+    ap.add_argument("--serve-jobs", type=int, default=48)
+    ap.add_argument("--workers", type=int, default=4)
     return ap.parse_args()
 
 
@@ -142,9 +146,66 @@ def workload(nv):
     return params, vec, point
 
 
-def evaluation(vec, point):
-    import oracle
-    return oracle.multilinear_extend(oracle.GOLDILOCKS2, vec, point.reshape(-1))
+def evaluation(ctx, vec, point):
+    import whir_gb300 as W
+    return W.multilinear_evaluate(ctx, W.GOLDILOCKS2, vec, point.reshape(-1))
+
+
+def batched_and_serving(args, dev):
+    """BASELINE-style batched workload (64 Goldilocks3 polynomials, d in {14..22}) proved back to
+    back on one context and batched over several contexts, then a Poisson serving trace of Goldilocks2
+    requests (d in {16..24}) at 70% of the measured batched capacity. Host wall clock (several streams
+    run at once); every batched / served proof is checked byte-identical to the back-to-back one."""
+    import whir_gb300 as W
+    from whir_gb300 import serving
+    ctx = W.Context(dev)
+    out = {}
+    jobs = serving.batched_workload(ctx, count=args.batch_jobs)
+    one = serving.BatchProver(dev, workers=1)
+    one.prove_all(jobs[:4])  # warm-up
+    t = time.perf_counter()
+    one.prove_all(jobs)
+    plain_s = time.perf_counter() - t
+    ref = [(j.narg, j.hints) for j in jobs]
+    one.close()
+    many = serving.BatchProver(dev, workers=args.workers)
+    many.prove_all(jobs[:8])
+    t = time.perf_counter()
+    many.prove_all(jobs)
+    batch_s = time.perf_counter() - t
+    many.close()
+    same = all((j.narg, j.hints) == r for j, r in zip(jobs, ref))
+    out["batched"] = {
+        "workload": "%d x WHIR commit+prove, Goldilocks3, d in {14,16,18,20,22}, Blake3, rate 1/2, k=4, sec 128 "
+                    "list decoding, 1-2 points" % len(jobs),
+        "proofs_per_s": len(jobs) / batch_s, "back_to_back_proofs_per_s": len(jobs) / plain_s,
+        "speedup_vs_back_to_back": plain_s / batch_s, "workers": args.workers, "bit_exact_vs_plain": same,
+        "timing": "host wall clock"}
+    sjobs = serving.serving_workload(ctx, count=args.serve_jobs)
+    cap = serving.BatchProver(dev, workers=args.workers)
+    cap.prove_all(sjobs[:8])
+    t = time.perf_counter()
+    cap.prove_all(sjobs)
+    cap_s = time.perf_counter() - t
+    cap.close()
+    sref = [(j.narg, j.hints) for j in sjobs]
+    capacity = len(sjobs) / cap_s
+    rate = 0.7 * capacity
+    srv = serving.ProofServer(dev, workers=args.workers, hbm_budget=150 << 30)
+    t = time.perf_counter()
+    lat = srv.run(sjobs, serving.poisson_arrivals(len(sjobs), rate, seed=6))
+    wall = time.perf_counter() - t
+    srv.close()
+    ctx.close()
+    out["serving"] = {
+        "workload": "%d requests, Goldilocks2 Blake3 k=4, d uniform over {16,18,20,22,24}, rate 1/2 or 1/4, 1-4 "
+                    "points, unique decoding; Poisson arrivals at 70%% of measured capacity; 150 GB HBM budget"
+                    % len(sjobs),
+        "capacity_proofs_per_s": capacity, "arrival_rate_per_s": rate, "p50_ms": float(np.percentile(lat, 50)) * 1e3,
+        "p99_ms": float(np.percentile(lat, 99)) * 1e3, "proofs_per_s": len(sjobs) / wall, "workers": args.workers,
+        "bit_exact_vs_plain": all((j.narg, j.hints) == r for j, r in zip(sjobs, sref)),
+        "timing": "host wall clock"}
+    return out
 
 
 def algorithmic_bytes(cfg_json, nv):
@@ -245,8 +306,8 @@ def run_gpu(args):
     torch.cuda.set_device(dev)
     nv = args.nv
     params, vec, point = workload(nv)
-    ev = evaluation(vec, point)
     ctx = W.Context(dev)
+    ev = evaluation(ctx, vec, point)
     cfg = W.Config("Goldilocks2", 1 << nv, params)
     cfg_json = cfg.json()
     stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=dev)
@@ -340,6 +401,7 @@ def run_gpu(args):
         roofline = {"bound": "integer", "kernel_family": fam, "achieved": None, "peak": peak, "unit": "GB/s",
                     "frac": None, "traffic": None, "avg_launch_ms": ms_f / calls_f}
     cpu = None if args.no_cpu_baseline else cpu_baseline(args, params, vec, point)
+    extra = {} if args.no_batch else batched_and_serving(args, dev)
     line = {
         "metric": "prove_ms_d%d_goldilocks2_blake3" % nv, "value": ms_per_proof_job, "unit": "ms",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(times)),
@@ -355,6 +417,7 @@ def run_gpu(args):
         "e2e": e2e,
         "gpu_launches": int(launches),
         "clocks": clocks,
+        **extra,
     }
     print(json.dumps(line))
 

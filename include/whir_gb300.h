@@ -162,6 +162,12 @@ int whir_geometric_accumulate(whir_ctx* ctx, int field, uint64_t* acc, size_t n,
 /* mixed_univariate_evaluate (src/algebra/mod.rs:105-129) for the embedding `field`. */
 int whir_univariate_evaluate(whir_ctx* ctx, int field, const uint64_t* coeffs, size_t n, const uint64_t* point,
                              uint64_t* out, uint32_t flags);
+/* Evaluation of the multilinear extension of n <= 2^nvars source values (implicitly zero-padded)
+ * at a target-field point: MultilinearExtension's Evaluate (linear_form/multilinear_extension.rs:
+ * 53-57 -> mixed_multilinear_extend, src/algebra/multilinear.rs:15-151). This is how callers compute
+ * the `evaluations` a statement passes to whir_prove. */
+int whir_multilinear_evaluate(whir_ctx* ctx, int field, const uint64_t* coeffs, size_t n, const uint64_t* point,
+                              size_t nvars, uint64_t* out, uint32_t flags);
 /* proof_of_work::Config::prove grinding (src/protocols/proof_of_work.rs:68-166): lowest nonce with
  * LE-u64(H(challenge || nonce_le || 0^24)[0..8]) <= threshold. */
 int whir_pow_grind(whir_ctx* ctx, const uint8_t engine_id[32], const uint8_t challenge[32], uint64_t threshold,

@@ -435,6 +435,18 @@ def univariate_evaluate(ctx, field, coeffs, point):
     return out
 
 
+def multilinear_evaluate(ctx, field, coeffs, point):
+    """MultilinearExtension(point).evaluate(embedding, coeffs) on the device."""
+    c = _as_u64(coeffs).reshape(-1)
+    p = _as_u64(point).reshape(-1)
+    L = TARGET_LIMBS[field]
+    out = np.zeros(L, np.uint64)
+    _check(load_library().whir_multilinear_evaluate(ctx._h, ctypes.c_int(field), _u64ptr(c),
+                                                    ctypes.c_size_t(c.size // SOURCE_LIMBS[field]), _u64ptr(p),
+                                                    ctypes.c_size_t(p.size // L), _u64ptr(out), ctypes.c_uint32(0)))
+    return out
+
+
 def pow_grind(ctx, engine, challenge, threshold):
     eid = np.frombuffer(ENGINES.get(engine, engine), dtype=np.uint8).copy()
     ch = np.frombuffer(bytes(challenge), dtype=np.uint8).copy()

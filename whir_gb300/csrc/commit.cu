@@ -325,13 +325,10 @@ int plan_encode(size_t n_msgs, size_t msg_len, size_t codeword_len, size_t eb, E
 
 template <class F, int KIND>
 static cudaError_t run_rows(const EncArgs<F>& a, unsigned grid, size_t smem, cudaStream_t s) {
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(encode_rows_kernel<F, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(ENC_SMEM_BUDGET + 32 * 1024));
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  // Set on every launch: the attribute is per device and this may run from several host threads.
+  cudaError_t e = cudaFuncSetAttribute(encode_rows_kernel<F, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(ENC_SMEM_BUDGET + 32 * 1024));
+  if (e != cudaSuccess) return e;
   encode_rows_kernel<F, KIND><<<grid, ENC_THREADS, smem, s>>>(a);
   note_launch();
   return cudaGetLastError();
@@ -373,13 +370,9 @@ cudaError_t launch_encode(const EncodePlan& p, const F* src, size_t n_msgs, size
   }
   // pass 1
   {
-    static bool configured = false;
-    if (!configured) {
-      cudaError_t e = cudaFuncSetAttribute(encode_cols_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)(ENC_SMEM_BUDGET + 32 * 1024));
-      if (e != cudaSuccess) return e;
-      configured = true;
-    }
+    cudaError_t ea = cudaFuncSetAttribute(encode_cols_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)(ENC_SMEM_BUDGET + 32 * 1024));
+    if (ea != cudaSuccess) return ea;
     EncArgs<F> c = a;
     c.src = src;
     c.dst = scratch;

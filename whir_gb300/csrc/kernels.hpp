@@ -118,6 +118,11 @@ template <class T, class S>
 cudaError_t launch_first_fold_compute_eq(const S* x, size_t n, T r, const T* tables, int nforms, int nv, T* a_out,
                                          T* b_out, T* partials, size_t* nparts, cudaStream_t s, T* out = nullptr,
                                          unsigned int* counter = nullptr);
+// sum_i map(x_i) * eq(point, i) for n <= 2^nv (implicit zero padding), from one eq table pair
+// (hi: 2^(nv/2) entries, then lo: 2^(nv - nv/2)); block sums -> partials (reduce_singles).
+template <class T, class S>
+cudaError_t launch_mle_dot(const S* x, size_t n, const T* tables, int nv, T* partials, size_t* nparts,
+                           cudaStream_t s);
 // Builds the eq table of `cnt` coordinates point[off..off+cnt) scaled by scalar (device arrays).
 template <class T>
 cudaError_t launch_eq_table(const T* point, int off, int cnt, T scalar, T* table, cudaStream_t s);

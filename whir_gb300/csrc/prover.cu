@@ -1414,6 +1414,34 @@ int whir_univariate_evaluate(whir_ctx* ctx, int field, const uint64_t* coeffs, s
   });
 }
 
+int whir_multilinear_evaluate(whir_ctx* ctx, int field, const uint64_t* coeffs, size_t n, const uint64_t* point,
+                              size_t nvars, uint64_t* out, uint32_t flags) {
+  return guarded([&] {
+    check_ctx(ctx);
+    if (nvars > 62 || (nvars < 62 && n > (1ull << nvars))) throw Error(WHIR_ERR_INVALID, "more values than 2^nvars");
+    return with_embedding(field, [&]<class S, class T>() {
+      T r = T::zero();
+      if (n) {
+        std::vector<T> pt = load_host<T>(point, nvars);
+        DBuf<S> hc;
+        const S* dc = device_vectors<S>(ctx, coeffs, n, flags, hc, false);
+        const int h = (int)nvars / 2, l = (int)nvars - h;
+        DBuf<T> dp(ctx, std::max<size_t>(nvars, 1)), tables(ctx, (1ull << h) + (1ull << l));
+        h2d(ctx, dp.p, pt.data(), nvars * sizeof(T));
+        CU(launch_eq_table<T>(dp.p, 0, h, T::one(), tables.p, ctx->stream));
+        CU(launch_eq_table<T>(dp.p, h, l, T::one(), tables.p + (1ull << h), ctx->stream));
+        DBuf<T> parts(ctx, 152 * 8 + 1), res(ctx, 1);
+        size_t np = 0;
+        CU((launch_mle_dot<T, S>(dc, n, tables.p, (int)nvars, parts.p, &np, ctx->stream)));
+        CU(launch_reduce_singles<T>(parts.p, np, res.p, ctx->stream));
+        d2h(ctx, &r, res.p, sizeof(T));
+      }
+      for (int d = 0; d < T::LIMBS; ++d) out[d] = r.coeff(d).v;
+      return 0;
+    });
+  });
+}
+
 int whir_pow_grind(whir_ctx* ctx, const uint8_t engine_id[32], const uint8_t challenge[32], uint64_t threshold,
                    uint64_t* nonce) {
   return guarded([&] {

@@ -502,6 +502,33 @@ cudaError_t launch_first_fold_compute_eq(const S* x, size_t n, T r, const T* tab
 }
 
 // ---------------------------------------------------------------------------------------------
+// Multilinear evaluation sum_i map(x_i) * eq(point, i) with the eq weights taken from one pair of
+// hi / lo tables (tables[0..2^h) and tables[2^h .. 2^h + 2^l)); block sums go to partials.
+// ---------------------------------------------------------------------------------------------
+template <class T, class S>
+__global__ void __launch_bounds__(SC_THREADS) mle_dot_kernel(const S* x, uint64_t n, const T* tables, int h, int l,
+                                                             T* partials) {
+  T acc = T::zero();
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    acc += Embed<T, S>::mul(eq_on_the_fly(tables, 1, h, l, i), x[i]);
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+}
+
+template <class T, class S>
+cudaError_t launch_mle_dot(const S* x, size_t n, const T* tables, int nv, T* partials, size_t* nparts,
+                           cudaStream_t s) {
+  size_t g = std::max<size_t>(1, std::min(SC_MAX_BLOCKS, (n + SC_THREADS - 1) / SC_THREADS));
+  mle_dot_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(x, n, tables, nv / 2, nv - nv / 2, partials);
+  note_launch();
+  *nparts = g;
+  return cudaGetLastError();
+}
+template cudaError_t launch_mle_dot<Gl, Gl>(const Gl*, size_t, const Gl*, int, Gl*, size_t*, cudaStream_t);
+template cudaError_t launch_mle_dot<Gl2, Gl>(const Gl*, size_t, const Gl2*, int, Gl2*, size_t*, cudaStream_t);
+template cudaError_t launch_mle_dot<Gl3, Gl>(const Gl*, size_t, const Gl3*, int, Gl3*, size_t*, cudaStream_t);
+
+// ---------------------------------------------------------------------------------------------
 // Lift + RLC
 // ---------------------------------------------------------------------------------------------
 template <class T, class S>
