@@ -22,16 +22,28 @@ def test_multilinear_evaluate_parity(ctx, orc, fname, fid, nv, n):
     assert np.array_equal(W.multilinear_evaluate(ctx, fid, x, pt), orc.multilinear_extend(fid, x, pt))
 
 
+def _max_pow_bits(params, field, nv):
+    c = W.Config(field, 1 << nv, params).json()
+    thr = [c["initial_sumcheck"]["round_pow_threshold"], c["initial_skip_pow_threshold"], c["final_pow_threshold"],
+           c["final_sumcheck"]["round_pow_threshold"]]
+    for r in c["rounds"]:
+        thr += [r["pow_threshold"], r["sumcheck"]["round_pow_threshold"]]
+    return max(64 - np.log2(float(t)) for t in thr)
+
+
 def _small_jobs(ctx, count, seed):
     r = Rng(seed)
     jobs = []
     for k in range(count):
         field = ("Goldilocks2", "Goldilocks3", "Goldilocks1")[k % 3]
         nv = 8 + int(r.raw(1)[0] % 7)
-        ud = bool(k % 2)
+        # A 64-bit field with list decoding needs ~40-bit fold proofs of work: Goldilocks1 jobs use
+        # unique decoding.
+        ud = bool(k % 2) or field == "Goldilocks1"
         params = W.ProtocolParameters(unique_decoding=ud, security_level=64, pow_bits=12,
                                       initial_folding_factor=2 + k % 3, folding_factor=2 + k % 2,
                                       starting_log_inv_rate=1 + k % 2, hash_id="Blake3")
+        assert _max_pow_bits(params, field, nv) <= 24, (field, nv, ud)
         jobs.append(serving.make_job(field, nv, params, 1 + k % 2, seed * 100 + k, ctx, session="mix-%d" % k))
     return jobs
 
