@@ -46,7 +46,7 @@ def test_config_and_transcript_without_device():
 
 def test_config_matches_oracle(orc):
     # The library's Config::new restatement and the oracle's agree on every derived value.
-    for field in ("Goldilocks1", "Goldilocks2", "Goldilocks3"):
+    for field in ("Goldilocks1", "Goldilocks2", "Goldilocks3", "Field192", "Field256"):
         for ud in (True, False):
             for nv, k, sec, powb, rate in ((10, 2, 32, 5, 1), (16, 4, 100, 20, 1), (20, 4, 128, 20, 2),
                                            (24, 4, 100, 20, 1), (13, 3, 80, 10, 3)):

@@ -11,7 +11,10 @@ from whir_gb300.inputs import Rng, field_elements
 
 pytestmark = pytest.mark.gpu
 
-FIELDS = [("Goldilocks1", W.GOLDILOCKS1), ("Goldilocks2", W.GOLDILOCKS2), ("Goldilocks3", W.GOLDILOCKS3)]
+FIELDS = [("Goldilocks1", W.GOLDILOCKS1), ("Goldilocks2", W.GOLDILOCKS2), ("Goldilocks3", W.GOLDILOCKS3),
+          ("Field192", W.FIELD192), ("Field256", W.FIELD256)]
+BASE_NAME = {"Goldilocks1": "Goldilocks1", "Goldilocks2": "Goldilocks1", "Goldilocks3": "Goldilocks1",
+             "Field192": "Field192", "Field256": "Field256"}
 
 
 @pytest.mark.parametrize("fname,fid", FIELDS)
@@ -28,6 +31,23 @@ def test_encode_parity(ctx, orc, fname, fid, n_msgs, msg_len, codeword_len):
     got = W.interleaved_encode(ctx, fid, msgs, codeword_len)
     exp = orc.interleaved_encode(fid, msgs, None, codeword_len)
     assert np.array_equal(got, exp)
+
+
+@pytest.mark.parametrize("fname,fid", FIELDS[3:])
+def test_encode_montgomery_fields_four_step(ctx, orc, fname, fid):
+    # Field192/Field256 rows are 24/32 bytes per element: the d=20, rate-1/4 initial shape (16 messages
+    # of 2^16 -> 2^18 rows) runs the four-step path; checked at spot rows against the oracle's
+    # univariate evaluation at the row's evaluation point.
+    rng = Rng(fid * 77)
+    L = W.TARGET_LIMBS[fid]
+    msgs = field_elements(fname, 16 << 16, rng=rng).reshape(16, 1 << 16, L)
+    cw = W.interleaved_encode(ctx, fid, msgs, 1 << 18)
+    rows = [0, 1, 5, 77777, (1 << 16) - 1, 1 << 16, (1 << 18) - 1]
+    pts = orc.evaluation_points(fid, 1 << 16, 1 << 18, np.array(rows, np.uint64))
+    for r, x in zip(rows, pts.reshape(len(rows), L)):
+        for m in (0, 9, 15):
+            v = orc.univariate_evaluate(fid, msgs[m].reshape(-1), x)
+            assert np.array_equal(cw[r, m], v)
 
 
 def test_encode_d24_initial_shape_properties(ctx, orc):
@@ -103,7 +123,7 @@ def test_geometric_accumulate_parity(ctx, orc, fname, fid, n, m):
 @pytest.mark.parametrize("n", [1, 2, 31, 32, 33, 8192, 100000, 1 << 20])
 def test_univariate_parity(ctx, orc, fid, fname, n):
     rng = Rng(n + 11 * fid)
-    c = rng.goldilocks(n)
+    c = field_elements(BASE_NAME[fname], n, rng=rng).reshape(-1)
     x = field_elements(fname, 1, rng=rng).reshape(-1)
     assert np.array_equal(W.univariate_evaluate(ctx, fid, c, x), orc.univariate_evaluate(fid, c, x))
 

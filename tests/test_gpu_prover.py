@@ -43,6 +43,12 @@ CASES = [
     ("Goldilocks2", 16, True, 4, 4, 3, 20, "Blake3", 100, 1, 1, 1, False),
     ("Goldilocks3", 16, False, 4, 4, 2, 20, "Blake3", 100, 1, 1, 1, False),
     ("Goldilocks2", 13, True, 1, 3, 1, 10, "Blake3", 64, 1, 1, 2, False),
+    ("Field192", 8, False, 4, 4, 2, 10, "Sha3", 32, 1, 1, 1, False),
+    ("Field256", 8, False, 4, 4, 1, 5, "Sha3", 32, 1, 2, 1, False),
+    ("Field192", 9, True, 3, 2, 1, 0, "Blake3", 40, 2, 1, 1, True),
+    ("Field256", 12, False, 4, 4, 4, 16, "Sha3", 128, 1, 1, 2, False),
+    ("Field192", 14, False, 4, 4, 4, 20, "Keccak", 128, 1, 1, 2, False),
+    ("Field256", 11, True, 2, 3, 2, 8, "Sha2", 64, 1, 1, 3, False),
 ]
 
 
@@ -88,6 +94,28 @@ def test_d20_goldilocks2_matches_oracle(ctx, orc):
     ref = orc.whir_prove(orc.GOLDILOCKS2, op, 20, "d20", vec, [pt], [], [[ev]])
     assert narg == ref.narg and hints == ref.hints
     assert orc.whir_verify(orc.GOLDILOCKS2, op, 20, "d20", 1, narg, hints, [pt], [], [[ev]])
+
+
+@pytest.mark.parametrize("field", ["Field256", "Field192"])
+def test_d20_montgomery_fields_match_oracle(ctx, orc, field):
+    # Multi-limb workload shape: d=20, SHA3 Merkle, rate 1/4, k=4, list decoding, security 128,
+    # pow 20, 4 uniform random evaluation points; byte-identical to the oracle and accepted by it.
+    params = W.ProtocolParameters(unique_decoding=False, security_level=128, pow_bits=20, hash_id="Sha3",
+                                  starting_log_inv_rate=2)
+    op = orc.make_params(unique_decoding=False, security_level=128, pow_bits=20, hash_id=orc.ENGINE_SHA3,
+                         starting_log_inv_rate=2)
+    f = orc.FIELD_IDS[field]
+    r = Rng(f * 20)
+    vec = field_elements(field, 1 << 20, rng=r).reshape(1, 1 << 20, -1)
+    pts = [field_elements(field, 20, rng=r).reshape(20, -1) for _ in range(4)]
+    evs = [[W.multilinear_evaluate(ctx, f, vec.reshape(-1), p.reshape(-1))] for p in pts]
+    for p, e in zip(pts, evs):
+        assert np.array_equal(e[0], orc.multilinear_extend(f, vec.reshape(-1), p.reshape(-1)))
+    narg, hints, claim, roots = gpu_prove(ctx, field, params, 20, "d20 " + field, vec, pts, [], evs, 1)
+    ref = orc.whir_prove(f, op, 20, "d20 " + field, vec, pts, [], evs)
+    assert b"".join(roots) == ref.roots
+    assert narg == ref.narg and hints == ref.hints
+    assert orc.whir_verify(f, op, 20, "d20 " + field, 1, narg, hints, pts, [], evs)
 
 
 def test_d24_goldilocks2_verifies(ctx, orc):

@@ -1,0 +1,410 @@
+// Interleaved Reed–Solomon encode kernels, shared by the translation units that instantiate them
+// for the Goldilocks family (commit.cu) and for the Montgomery fields (commit_mont.cu).
+//
+// Encode (reference ntt/cooley_tukey.rs:411-477). For message m, coset c in [0, K) and t in [0, C)
+// the codeword row c*C + t, column m holds P_m(w_N^c * w_C^t) = NTT_C(x_j * w_N^(c j))[t]: the
+// coset twist is applied while loading, the size-C NTT runs in shared memory (radix-8/4/2
+// decimation-in-frequency steps in registers, natural order in, bit-reversed order out), and each
+// CTA finishes whole codeword rows so it can write them with coalesced stores and hash them
+// straight from shared memory (matrix_commit.rs:211-232 leaf hashing, merkle_tree.rs:82-127 leaves).
+// Large C is split four-step as C = C1 * C2: pass 1 (cols) runs NTT_C1 over strided columns,
+// applies the w_C^(j2 k1) twiddles and writes an intermediate; pass 2 (rows) runs NTT_C2 over
+// contiguous rows and emits codeword rows t = k1 + C1 * k2.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "field.cuh"
+#include "hash.cuh"
+#include "kernels.hpp"
+#include "roots.cuh"
+
+namespace whir {
+
+static constexpr int ENC_THREADS = 256;
+static constexpr size_t ENC_SMEM_BUDGET = 64 * 1024;  // data bytes per CTA
+static constexpr int ENC_MAX_LOGN_SMEM = 12;          // largest in-CTA NTT
+// Dynamic shared memory limit set on the encode kernels: the data tile plus up to half its size in
+// twiddles (n/2 base elements for a size-n NTT) plus alignment slack.
+static constexpr size_t ENC_SMEM_ATTR = ENC_SMEM_BUDGET + ENC_SMEM_BUDGET / 2 + 256;
+
+
+// LOGR consecutive decimation-in-frequency stages done in registers. The current sub-blocks have
+// size B = 2^logB; a work item (vector v, sub-block blk, offset j < B/R) owns the R = 2^LOGR
+// elements at offsets j + k*B/R, k < R, which are exactly the elements those stages combine.
+// Stage st pairs k with k + R/2^(st+1) and multiplies the difference by w_(2h)^(offset mod 2h),
+// 2h = B / 2^st, read from tw[q] = w_n^q.
+template <class F, int LOGR>
+__device__ __forceinline__ void dif_step(F* s, int logn, int logB, int nvec, int lognvec, int vs, int es,
+                                         bool vec_fastest, const typename F::Base* tw) {
+  constexpr int R = 1 << LOGR;
+  const int logstride = logB - LOGR;
+  const int stride = 1 << logstride;
+  const int items_log = logn - LOGR;  // work items per vector = n / R
+  const int total = nvec << items_log;
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    int v, it;
+    if (vec_fastest) {
+      v = t & (nvec - 1);
+      it = t >> lognvec;
+    } else {
+      v = t >> items_log;
+      it = t & ((1 << items_log) - 1);
+    }
+    const int blk = it >> logstride, j = it & (stride - 1);
+    F* base = s + v * vs + (((blk << logB) + j) * es);
+    const int kstep = stride * es;
+    F x[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) x[k] = base[k * kstep];
+#pragma unroll
+    for (int st = 0; st < LOGR; ++st) {
+      const int half = R >> (st + 1);
+      const int log2h = logB - st;
+      const int tws = logn - log2h;
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        if (k & half) continue;
+        const int pos = (j + k * stride) & ((1 << log2h) - 1);
+        const F u = x[k], w = x[k + half];
+        x[k] = u + w;
+        x[k + half] = (u - w).mul_base(tw[pos << tws]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) base[k * kstep] = x[k];
+  }
+  __syncthreads();
+}
+
+// In-place DIF NTT of nvec vectors of size 2^logn in shared memory; element i of vector v lives at
+// s[v*vs + i*es]. Output index k ends up at position brev(k). Stages are processed three at a time
+// in registers (radix 8), with a radix-4 / radix-2 step for the remainder.
+template <class F>
+__device__ void smem_ntt_dif(F* s, int logn, int nvec, int vs, int es, bool vec_fastest, const typename F::Base* tw) {
+  int lognvec = 0;
+  while ((1 << lognvec) < nvec) ++lognvec;
+  int logB = logn;
+  while (logB >= 3) {
+    dif_step<F, 3>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
+    logB -= 3;
+  }
+  if (logB == 2) dif_step<F, 2>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
+  if (logB == 1) dif_step<F, 1>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
+}
+
+// 32-bit little-endian words of an element's u64 limbs (the element must already be canonical).
+template <class F>
+__device__ __forceinline__ void push_elem_words(const F& x, uint32_t* w) {
+  const uint64_t* l = reinterpret_cast<const uint64_t*>(&x);
+#pragma unroll
+  for (int i = 0; i < F::LIMBS; ++i) {
+    w[2 * i] = (uint32_t)l[i];
+    w[2 * i + 1] = (uint32_t)(l[i] >> 32);
+  }
+}
+
+template <class F>
+struct EncArgs {
+  const F* src;  // rows mode 0: messages; rows mode 1: intermediate; cols: messages
+  F* dst;        // rows: codeword; cols: intermediate
+  uint32_t* leaves;
+  uint64_t msg_len;
+  uint64_t K;  // number of cosets
+  int M;       // messages = codeword columns
+  int logC, logN, logC1, logC2;
+  int mode;    // rows kernel: 0 single pass, 1 four-step pass 2
+  int G;       // cosets per CTA (rows mode 0)
+  int W;       // columns per CTA (cols kernel)
+  RootTab rt;
+};
+
+// Produces whole codeword rows: writes them and (optionally) their leaf digests.
+template <class F, int KIND>
+__global__ void __launch_bounds__(ENC_THREADS) encode_rows_kernel(EncArgs<F> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  F* s = reinterpret_cast<F*>(smem_raw);
+  const int M = a.M;
+  const int logn = a.mode == 0 ? a.logC : a.logC2;
+  const int n = 1 << logn;
+  const int nvec = a.mode == 0 ? a.G * M : M;
+  const int R = a.mode == 0 ? a.G * n : n;  // rows produced by this CTA
+  typedef typename F::Base B;
+  B* tw = reinterpret_cast<B*>(smem_raw + (size_t)nvec * n * sizeof(F));
+  const uint64_t C = 1ull << a.logC, N = 1ull << a.logN;
+  for (int k = threadIdx.x; k < (n >> 1); k += blockDim.x) tw[k] = root_pow<B>(a.rt, logn, (uint64_t)k);
+
+  uint64_t c_base = 0, k1 = 0;
+  if (a.mode == 0) {
+    c_base = (uint64_t)blockIdx.x * a.G;
+    for (int idx = threadIdx.x; idx < nvec * n; idx += blockDim.x) {
+      const int vec = idx >> logn, j = idx & (n - 1);
+      const int g = vec / M, m = vec - g * M;
+      const uint64_t c = c_base + g;
+      F x = (uint64_t)j < a.msg_len ? a.src[(uint64_t)m * a.msg_len + j] : F::zero();
+      if (c != 0 && j != 0) x = x.mul_base(root_pow<B>(a.rt, a.logN, (c * (uint64_t)j) & (N - 1)));
+      s[idx] = x;
+    }
+  } else {
+    const uint64_t C1 = 1ull << a.logC1;
+    c_base = blockIdx.x >> a.logC1;
+    k1 = blockIdx.x & (C1 - 1);
+    for (int idx = threadIdx.x; idx < M * n; idx += blockDim.x) {
+      const int m = idx >> logn, j2 = idx & (n - 1);
+      s[idx] = a.src[((((uint64_t)m * a.K + c_base) << a.logC1) + k1) * n + j2];
+    }
+  }
+  __syncthreads();
+  smem_ntt_dif<F>(s, logn, nvec, n, 1, false, tw);
+
+  // Coalesced row stores: consecutive threads write consecutive columns of consecutive rows.
+  for (int idx = threadIdx.x; idx < R * M; idx += blockDim.x) {
+    const int rho = idx / M, m = idx - rho * M;
+    uint64_t row;
+    int sidx;
+    if (a.mode == 0) {
+      const int g = rho >> logn, t = rho & (n - 1);
+      row = (c_base + g) * C + t;
+      sidx = ((g * M + m) << logn) + brev(t, logn);
+    } else {
+      row = c_base * C + k1 + ((uint64_t)rho << a.logC1);
+      sidx = (m << logn) + brev(rho, logn);
+    }
+    a.dst[row * M + m] = s[sidx];
+  }
+  if (a.leaves == nullptr) return;
+  if constexpr (!Canon<F>::IDENTITY) {
+    // Leaves hash canonical bytes: convert the tile in place once every row has been stored.
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < nvec * n; idx += blockDim.x) {
+      uint64_t c[F::LIMBS];
+      Canon<F>::to(s[idx], c);
+      uint64_t* d = reinterpret_cast<uint64_t*>(&s[idx]);
+#pragma unroll
+      for (int q = 0; q < F::LIMBS; ++q) d[q] = c[q];
+    }
+    __syncthreads();
+  }
+  // One thread per row: hash the row's canonical little-endian bytes.
+  for (int rho = threadIdx.x; rho < R; rho += blockDim.x) {
+    uint64_t row;
+    int base, g = 0, t = rho;
+    if (a.mode == 0) {
+      g = rho >> logn;
+      t = rho & (n - 1);
+      row = (c_base + g) * C + t;
+      base = ((g * M) << logn) + brev(t, logn);
+    } else {
+      row = c_base * C + k1 + ((uint64_t)rho << a.logC1);
+      base = brev(rho, logn);
+    }
+    uint32_t out[8];
+    if constexpr (KIND == HASH_BLAKE3) {
+      // Message blocks assembled in registers (static indices) straight from shared memory:
+      // block b holds u64 limbs 8b .. 8b+7 of the row (limb L = limb L % LIMBS of column L / LIMBS).
+      const int limbs = M * F::LIMBS;
+      const int nblocks = limbs == 0 ? 1 : (limbs + 7) / 8;
+      blake3_iv(out);
+      for (int b = 0; b < nblocks; ++b) {
+        uint32_t mw[16];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int L = b * 8 + q;
+          uint64_t limb = 0;
+          if (L < limbs) {
+            const int col = L / F::LIMBS, part = L - col * F::LIMBS;
+            limb = reinterpret_cast<const uint64_t*>(&s[base + (col << logn)])[part];
+          }
+          mw[2 * q] = (uint32_t)limb;
+          mw[2 * q + 1] = (uint32_t)(limb >> 32);
+        }
+        const bool last = b == nblocks - 1;
+        const uint32_t blen = last ? (uint32_t)(limbs - b * 8) * 8 : 64;
+        const uint32_t flags = (b == 0 ? B3_CHUNK_START : 0) | (last ? (B3_CHUNK_END | B3_ROOT) : 0);
+        blake3_compress_cv(out, mw, 0, 0, blen, flags);
+      }
+    } else {
+      WordHasher<KIND> h;
+      h.init((uint32_t)(M * F::LIMBS * 8));
+      for (int m = 0; m < M; ++m) {
+        uint32_t w[2 * F::LIMBS];
+        push_elem_words<F>(s[base + (m << logn)], w);
+#pragma unroll
+        for (int q = 0; q < 2 * F::LIMBS; ++q) h.push(w[q]);
+      }
+      h.finish(out);
+    }
+    uint4* dstw = reinterpret_cast<uint4*>(a.leaves + row * 8);
+    dstw[0] = make_uint4(out[0], out[1], out[2], out[3]);
+    dstw[1] = make_uint4(out[4], out[5], out[6], out[7]);
+  }
+}
+
+// Four-step pass 1: NTT_C1 over columns j2 of the (C1 x C2) view of each twisted message,
+// multiplied by w_C^(j2 k1); intermediate layout [m][c][k1][j2].
+template <class F>
+__global__ void __launch_bounds__(ENC_THREADS) encode_cols_kernel(EncArgs<F> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  F* s = reinterpret_cast<F*>(smem_raw);
+  const int logn = a.logC1, n = 1 << logn, W = a.W;
+  typedef typename F::Base B;
+  B* tw = reinterpret_cast<B*>(smem_raw + (size_t)W * n * sizeof(F));
+  const uint64_t C2 = 1ull << a.logC2, N = 1ull << a.logN;
+  const uint64_t tiles = C2 / W;
+  const uint64_t tile = blockIdx.x % tiles;
+  const uint64_t mc = blockIdx.x / tiles;  // m * K + c
+  const uint64_t c = mc % a.K, m = mc / a.K;
+  for (int k = threadIdx.x; k < (n >> 1); k += blockDim.x) tw[k] = root_pow<B>(a.rt, logn, (uint64_t)k);
+  for (int idx = threadIdx.x; idx < n * W; idx += blockDim.x) {
+    const int j1 = idx / W, w = idx - j1 * W;
+    const uint64_t j = ((uint64_t)j1 << a.logC2) + tile * W + w;
+    F x = j < a.msg_len ? a.src[m * a.msg_len + j] : F::zero();
+    if (c != 0 && j != 0) x = x.mul_base(root_pow<B>(a.rt, a.logN, (c * j) & (N - 1)));
+    s[idx] = x;
+  }
+  __syncthreads();
+  smem_ntt_dif<F>(s, logn, W, 1, W, true, tw);
+  for (int idx = threadIdx.x; idx < n * W; idx += blockDim.x) {
+    const int k1 = idx / W, w = idx - k1 * W;
+    const uint64_t j2 = tile * W + w;
+    F v = s[brev(k1, logn) * W + w];
+    const uint64_t e = j2 * (uint64_t)k1;
+    if (e) v = v.mul_base(root_pow<B>(a.rt, a.logC, e));
+    a.dst[((mc << a.logC1) + k1) * C2 + j2] = v;
+  }
+}
+
+template <class F, int KIND>
+static cudaError_t run_rows(const EncArgs<F>& a, unsigned grid, size_t smem, cudaStream_t s) {
+  // Set on every launch: the attribute is per device and this may run from several host threads.
+  cudaError_t e = cudaFuncSetAttribute(encode_rows_kernel<F, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)ENC_SMEM_ATTR);
+  if (e != cudaSuccess) return e;
+  encode_rows_kernel<F, KIND><<<grid, ENC_THREADS, smem, s>>>(a);
+  note_launch();
+  return cudaGetLastError();
+}
+
+template <class F>
+static cudaError_t dispatch_rows(const EncArgs<F>& a, int kind, unsigned grid, size_t smem, cudaStream_t s) {
+  switch (kind) {
+    case HASH_BLAKE3: return run_rows<F, HASH_BLAKE3>(a, grid, smem, s);
+    case HASH_SHA2: return run_rows<F, HASH_SHA2>(a, grid, smem, s);
+    case HASH_SHA3: return run_rows<F, HASH_SHA3>(a, grid, smem, s);
+    case HASH_KECCAK: return run_rows<F, HASH_KECCAK>(a, grid, smem, s);
+    default: return run_rows<F, HASH_COPY>(a, grid, smem, s);
+  }
+}
+
+template <class F>
+cudaError_t launch_encode(const EncodePlan& p, const F* src, size_t n_msgs, size_t msg_len, F* dst,
+                          uint32_t* leaves, int hash_kind, F* scratch, RootTab rt, cudaStream_t s) {
+  // Every root index below is taken modulo the codeword length, which must divide 2^log_order.
+  if (p.logN > rt.log_order || p.logN > 32) return cudaErrorInvalidValue;
+  EncArgs<F> a;
+  a.leaves = leaves;
+  a.msg_len = msg_len;
+  a.M = (int)n_msgs;
+  a.logC = p.logC;
+  a.logN = p.logN;
+  a.logC1 = p.logC1;
+  a.logC2 = p.logC2;
+  a.K = 1ull << (p.logN - p.logC);
+  a.G = p.cosets_per_cta;
+  a.W = p.cols_per_cta;
+  a.rt = rt;
+  if (p.mode == 0) {
+    a.mode = 0;
+    a.src = src;
+    a.dst = dst;
+    const size_t n = 1ull << p.logC;
+    const size_t smem = (size_t)a.G * n_msgs * n * sizeof(F) + (n / 2) * sizeof(typename F::Base) + 16;
+    return dispatch_rows<F>(a, hash_kind, (unsigned)(a.K / a.G), smem, s);
+  }
+  // pass 1
+  {
+    cudaError_t ea = cudaFuncSetAttribute(encode_cols_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)ENC_SMEM_ATTR);
+    if (ea != cudaSuccess) return ea;
+    EncArgs<F> c = a;
+    c.src = src;
+    c.dst = scratch;
+    c.leaves = nullptr;
+    const size_t C1 = 1ull << p.logC1, C2 = 1ull << p.logC2;
+    const size_t smem = (size_t)a.W * C1 * sizeof(F) + (C1 / 2) * sizeof(typename F::Base) + 16;
+    const size_t grid = n_msgs * a.K * (C2 / a.W);
+    encode_cols_kernel<F><<<(unsigned)grid, ENC_THREADS, smem, s>>>(c);
+    note_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  // pass 2
+  a.mode = 1;
+  a.src = scratch;
+  a.dst = dst;
+  const size_t C1 = 1ull << p.logC1, C2 = 1ull << p.logC2;
+  const size_t smem = n_msgs * C2 * sizeof(F) + (C2 / 2) * sizeof(typename F::Base) + 16;
+  return dispatch_rows<F>(a, hash_kind, (unsigned)(a.K * C1), smem, s);
+}
+
+// Opening gathers
+// ---------------------------------------------------------------------------------------------
+template <class F>
+__global__ void gather_rows_kernel(const F* matrix, uint64_t cols, const uint64_t* idx, uint64_t n, F* out) {
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n * cols; t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = t / cols, c = t - i * cols;
+    out[t] = matrix[idx[i] * cols + c];
+  }
+}
+template <class F>
+cudaError_t launch_gather_rows(const F* matrix, size_t cols, const uint64_t* idx, size_t n, F* out, cudaStream_t s) {
+  if (n * cols == 0) return cudaSuccess;
+  unsigned grid = (unsigned)std::min<size_t>((n * cols + 255) / 256, 4096);
+  gather_rows_kernel<F><<<grid, 256, 0, s>>>(matrix, cols, idx, n, out);
+  note_launch();
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Canonical <-> in-memory form (Montgomery for Field192/Field256)
+// ---------------------------------------------------------------------------------------------
+template <class F, bool TO_INTERNAL>
+__global__ void convert_kernel(F* v, uint64_t n) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t* w = reinterpret_cast<uint64_t*>(v + i);
+    if constexpr (TO_INTERNAL) {
+      v[i] = Canon<F>::from(w);
+    } else {
+      uint64_t c[F::LIMBS];
+      Canon<F>::to(v[i], c);
+#pragma unroll
+      for (int q = 0; q < F::LIMBS; ++q) w[q] = c[q];
+    }
+  }
+}
+template <class F, bool TO_INTERNAL>
+cudaError_t launch_convert(F* v, size_t n, cudaStream_t s) {
+  if (Canon<F>::IDENTITY || n == 0) return cudaSuccess;
+  const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 16);
+  convert_kernel<F, TO_INTERNAL><<<grid, 256, 0, s>>>(v, n);
+  note_launch();
+  return cudaGetLastError();
+}
+template <class F>
+cudaError_t launch_to_internal(F* v, size_t n, cudaStream_t s) {
+  return launch_convert<F, true>(v, n, s);
+}
+template <class F>
+cudaError_t launch_to_canonical(F* v, size_t n, cudaStream_t s) {
+  return launch_convert<F, false>(v, n, s);
+}
+
+#define WHIR_ENCODE_INST(F)                                                                                      \
+  template cudaError_t launch_encode<F>(const EncodePlan&, const F*, size_t, size_t, F*, uint32_t*, int, F*, RootTab, \
+                                        cudaStream_t);                                                           \
+  template cudaError_t launch_gather_rows<F>(const F*, size_t, const uint64_t*, size_t, F*, cudaStream_t);       \
+  template cudaError_t launch_to_internal<F>(F*, size_t, cudaStream_t);                                         \
+  template cudaError_t launch_to_canonical<F>(F*, size_t, cudaStream_t);
+
+}  // namespace whir

@@ -301,6 +301,264 @@ struct Gl3 {
   }
 };
 
+// ---------------------------------------------------------------------------------------------
+// Multi-limb prime fields in Montgomery form (R = 2^(64N)), as ark-ff's MontBackend stores them:
+//   Field192  p = 3801539170989320091464968600173246866371124347557388484609, generator 3
+//   Field256  BN254 scalar field, generator 5 (fields.rs:65-77)
+// Elements live in Montgomery form in memory (host and device); the C ABI, the transcript and leaf
+// hashing use canonical little-endian limbs (to_canonical / from_canonical).
+// ---------------------------------------------------------------------------------------------
+typedef unsigned __int128 u128_t;
+
+struct F192Params {
+  static constexpr int N = 3;
+  static constexpr int BYTES = 24;  // ceil(192 / 8)
+  WHIR_HD static uint64_t p(int i) {
+    return i == 0 ? 0x5887000000000001ULL : (i == 1 ? 0x0ad0a439abc2c817ULL : 0x9b09ebbd813f1e17ULL);
+  }
+  WHIR_HD static uint64_t r2(int i) {
+    return i == 0 ? 0xe7d9d9a32bc43105ULL : (i == 1 ? 0x9b5537d38879c40aULL : 0x6c2a69f7d53e03c3ULL);
+  }
+  WHIR_HD static uint64_t one(int i) {
+    return i == 0 ? 0xa778ffffffffffffULL : (i == 1 ? 0xf52f5bc6543d37e8ULL : 0x64f614427ec0e1e8ULL);
+  }
+  static constexpr uint64_t PINV = 0x5886ffffffffffffULL;  // -p^{-1} mod 2^64
+  static constexpr uint64_t GENERATOR = 3;
+  static constexpr int TWO_ADICITY = 48;
+  static constexpr uint64_t SMALL_ORDER = 1;  // no 3-power subgroup used by the NTT engine
+};
+struct F256Params {
+  static constexpr int N = 4;
+  static constexpr int BYTES = 32;  // ceil(254 / 8)
+  WHIR_HD static uint64_t p(int i) {
+    switch (i) {
+      case 0: return 0x43e1f593f0000001ULL;
+      case 1: return 0x2833e84879b97091ULL;
+      case 2: return 0xb85045b68181585dULL;
+      default: return 0x30644e72e131a029ULL;
+    }
+  }
+  WHIR_HD static uint64_t r2(int i) {
+    switch (i) {
+      case 0: return 0x1bb8e645ae216da7ULL;
+      case 1: return 0x53fe3ab1e35c59e3ULL;
+      case 2: return 0x8c49833d53bb8085ULL;
+      default: return 0x0216d0b17f4e44a5ULL;
+    }
+  }
+  WHIR_HD static uint64_t one(int i) {
+    switch (i) {
+      case 0: return 0xac96341c4ffffffbULL;
+      case 1: return 0x36fc76959f60cd29ULL;
+      case 2: return 0x666ea36f7879462eULL;
+      default: return 0x0e0a77c19a07df2fULL;
+    }
+  }
+  static constexpr uint64_t PINV = 0xc2e1f593efffffffULL;
+  static constexpr uint64_t GENERATOR = 5;
+  static constexpr int TWO_ADICITY = 28;
+  static constexpr uint64_t SMALL_ORDER = 9;  // 3^2 (small_subgroup_base 3, power 2)
+};
+
+template <class P>
+struct MontField {
+  static constexpr int N = P::N;
+  uint64_t l[N];
+  static constexpr int DEG = 1;
+  static constexpr int LIMBS = N;  // u64 words per element (storage)
+  typedef MontField Base;
+
+  WHIR_HD static MontField zero() {
+    MontField r;
+    for (int i = 0; i < N; ++i) r.l[i] = 0;
+    return r;
+  }
+  WHIR_HD static MontField one() {
+    MontField r;
+    for (int i = 0; i < N; ++i) r.l[i] = P::one(i);
+    return r;
+  }
+  WHIR_HD static MontField from_base(const MontField& b) { return b; }
+  WHIR_HD MontField coeff(int) const { return *this; }
+
+  WHIR_HD static bool geq_p(const uint64_t* a) {
+    for (int i = N - 1; i >= 0; --i) {
+      const uint64_t pi = P::p(i);
+      if (a[i] != pi) return a[i] > pi;
+    }
+    return true;
+  }
+  WHIR_HD static void sub_p(uint64_t* a) {
+    uint64_t borrow = 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      const u128_t d = (u128_t)a[i] - P::p(i) - borrow;
+      a[i] = (uint64_t)d;
+      borrow = (uint64_t)(d >> 64) & 1;
+    }
+  }
+  // CIOS Montgomery multiplication: a * b * R^{-1} mod p.
+  WHIR_HD static MontField mont_mul(const uint64_t* a, const uint64_t* b) {
+    uint64_t t[N + 2];
+    for (int i = 0; i < N + 2; ++i) t[i] = 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      uint64_t carry = 0;
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        const u128_t s = (u128_t)a[j] * b[i] + t[j] + carry;
+        t[j] = (uint64_t)s;
+        carry = (uint64_t)(s >> 64);
+      }
+      u128_t s = (u128_t)t[N] + carry;
+      t[N] = (uint64_t)s;
+      t[N + 1] = (uint64_t)(s >> 64);
+      const uint64_t m = t[0] * P::PINV;
+      u128_t s2 = (u128_t)m * P::p(0) + t[0];
+      carry = (uint64_t)(s2 >> 64);
+#pragma unroll
+      for (int j = 1; j < N; ++j) {
+        const u128_t s3 = (u128_t)m * P::p(j) + t[j] + carry;
+        t[j - 1] = (uint64_t)s3;
+        carry = (uint64_t)(s3 >> 64);
+      }
+      const u128_t s4 = (u128_t)t[N] + carry;
+      t[N - 1] = (uint64_t)s4;
+      t[N] = t[N + 1] + (uint64_t)(s4 >> 64);
+    }
+    MontField r;
+    for (int i = 0; i < N; ++i) r.l[i] = t[i];
+    if (t[N] || geq_p(r.l)) sub_p(r.l);
+    return r;
+  }
+  WHIR_HD friend MontField operator*(const MontField& a, const MontField& b) { return mont_mul(a.l, b.l); }
+  WHIR_HD friend MontField operator+(const MontField& a, const MontField& b) {
+    MontField r;
+    uint64_t carry = 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      const u128_t s = (u128_t)a.l[i] + b.l[i] + carry;
+      r.l[i] = (uint64_t)s;
+      carry = (uint64_t)(s >> 64);
+    }
+    if (carry || geq_p(r.l)) sub_p(r.l);
+    return r;
+  }
+  WHIR_HD friend MontField operator-(const MontField& a, const MontField& b) {
+    MontField r;
+    uint64_t borrow = 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      const u128_t d = (u128_t)a.l[i] - b.l[i] - borrow;
+      r.l[i] = (uint64_t)d;
+      borrow = (uint64_t)(d >> 64) & 1;
+    }
+    if (borrow) {
+      uint64_t carry = 0;
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        const u128_t s = (u128_t)r.l[i] + P::p(i) + carry;
+        r.l[i] = (uint64_t)s;
+        carry = (uint64_t)(s >> 64);
+      }
+    }
+    return r;
+  }
+  WHIR_HD MontField operator-() const { return zero() - *this; }
+  WHIR_HD MontField& operator+=(const MontField& b) { *this = *this + b; return *this; }
+  WHIR_HD MontField& operator-=(const MontField& b) { *this = *this - b; return *this; }
+  WHIR_HD MontField& operator*=(const MontField& b) { *this = *this * b; return *this; }
+  WHIR_HD bool operator==(const MontField& b) const {
+    for (int i = 0; i < N; ++i)
+      if (l[i] != b.l[i]) return false;
+    return true;
+  }
+  WHIR_HD bool operator!=(const MontField& b) const { return !(*this == b); }
+  WHIR_HD bool is_zero() const {
+    uint64_t o = 0;
+    for (int i = 0; i < N; ++i) o |= l[i];
+    return o == 0;
+  }
+  WHIR_HD MontField mul_base(const MontField& b) const { return *this * b; }
+  WHIR_HD MontField dbl() const { return *this + *this; }
+  WHIR_HD MontField sqr() const { return *this * *this; }
+  WHIR_HD MontField pow(uint64_t e) const {
+    MontField r = one(), a = *this;
+    while (e) {
+      if (e & 1) r = r * a;
+      a = a * a;
+      e >>= 1;
+    }
+    return r;
+  }
+  // base^e for a little-endian multi-limb exponent
+  WHIR_HD MontField pow_limbs(const uint64_t* e, int ne) const {
+    MontField r = one();
+    for (int i = ne - 1; i >= 0; --i)
+      for (int b = 63; b >= 0; --b) {
+        r = r * r;
+        if ((e[i] >> b) & 1) r = r * *this;
+      }
+    return r;
+  }
+  WHIR_HD MontField inv() const {
+    uint64_t e[N];
+    uint64_t borrow = 2;
+    for (int i = 0; i < N; ++i) {
+      const uint64_t pi = P::p(i);
+      e[i] = pi - borrow;
+      borrow = pi < borrow ? 1 : 0;
+    }
+    return pow_limbs(e, N);
+  }
+  WHIR_HD static MontField from_canonical(const uint64_t* c) {
+    uint64_t r2[N];
+    for (int i = 0; i < N; ++i) r2[i] = P::r2(i);
+    return mont_mul(c, r2);
+  }
+  WHIR_HD void to_canonical(uint64_t* out) const {
+    uint64_t one_c[N];
+    for (int i = 0; i < N; ++i) one_c[i] = i == 0 ? 1 : 0;
+    MontField r = mont_mul(l, one_c);
+    for (int i = 0; i < N; ++i) out[i] = r.l[i];
+  }
+  WHIR_HD static bool canonical_ok(const uint64_t* c) { return !geq_p(c); }
+};
+
+typedef MontField<F192Params> F192;
+typedef MontField<F256Params> F256;
+
+// Canonical conversion for every field type: element -> F::LIMBS canonical u64 limbs and back
+// (identity for the Goldilocks family, whose elements are stored canonically).
+template <class F>
+struct Canon {
+  WHIR_HD static void to(const F& x, uint64_t* out) {
+    const uint64_t* w = reinterpret_cast<const uint64_t*>(&x);
+    for (int i = 0; i < F::LIMBS; ++i) out[i] = w[i];
+  }
+  WHIR_HD static F from(const uint64_t* in) {
+    F x;
+    uint64_t* w = reinterpret_cast<uint64_t*>(&x);
+    for (int i = 0; i < F::LIMBS; ++i) w[i] = in[i];
+    return x;
+  }
+  WHIR_HD static bool ok(const uint64_t* in) {
+    for (int i = 0; i < F::LIMBS; ++i)
+      if (in[i] >= GL_P) return false;
+    return true;
+  }
+  static constexpr int BASE_BYTES = 8;  // encoded bytes per base coefficient
+  static constexpr bool IDENTITY = true;
+};
+template <class P>
+struct Canon<MontField<P>> {
+  WHIR_HD static void to(const MontField<P>& x, uint64_t* out) { x.to_canonical(out); }
+  WHIR_HD static MontField<P> from(const uint64_t* in) { return MontField<P>::from_canonical(in); }
+  WHIR_HD static bool ok(const uint64_t* in) { return MontField<P>::canonical_ok(in); }
+  static constexpr int BASE_BYTES = P::BYTES;
+  static constexpr bool IDENTITY = false;
+};
+
 // Embedding helpers (reference src/algebra/embedding.rs:126-153).
 template <class T, class S>
 struct Embed {

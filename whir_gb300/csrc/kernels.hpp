@@ -15,11 +15,21 @@ namespace whir {
 uint64_t kernel_launches();
 void note_launch();
 
-// Powers of the 2^32-th root of unity of Goldilocks: lo[i] = w^i, hi[i] = w^(i * 2^16), i < 2^16.
+// Powers of the 2^log_order-th root of unity w of a base prime field, stored as base-field elements
+// (Montgomery form for Field192/Field256): lo[i] = w^i (i < 2^16), hi[i] = w^(i * 2^16)
+// (i < 2^(log_order - 16)).
 struct RootTab {
   const uint64_t* lo;
   const uint64_t* hi;
+  int log_order;
 };
+
+// In-place conversion between the canonical limbs of the C ABI and the in-memory form of F
+// (a no-op for the Goldilocks family; Montgomery form for Field192/Field256).
+template <class F>
+cudaError_t launch_to_internal(F* v, size_t n, cudaStream_t s);
+template <class F>
+cudaError_t launch_to_canonical(F* v, size_t n, cudaStream_t s);
 
 // Shape of one interleaved Reed–Solomon encode (reference cooley_tukey.rs:411-477).
 struct EncodePlan {

@@ -195,22 +195,39 @@ inline std::vector<uint8_t> cbor_text(const std::string& s) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// Goldilocks-family codecs (8 little-endian bytes per base coefficient)
+// Element codecs: ArkFieldEncoder bytes are the canonical little-endian bytes of each base
+// coefficient, 8 per Goldilocks coefficient, 24 for Field192 and 32 for Field256 (exactly the
+// canonical u64 limbs of the element in every supported field).
 // ---------------------------------------------------------------------------------------------
 template <class F>
 inline void elem_bytes(const F& x, uint8_t* out) {
-  for (int d = 0; d < F::DEG; ++d) {
-    uint64_t v = x.coeff(d).v;
-    for (int i = 0; i < 8; ++i) out[8 * d + i] = (uint8_t)(v >> (8 * i));
-  }
+  static_assert(F::LIMBS * 8 == F::DEG * Canon<F>::BASE_BYTES, "encoded size must equal the limb size");
+  uint64_t c[F::LIMBS];
+  Canon<F>::to(x, c);
+  for (int d = 0; d < F::LIMBS; ++d)
+    for (int i = 0; i < 8; ++i) out[8 * d + i] = (uint8_t)(c[d] >> (8 * i));
 }
 template <class F>
 inline void send_elem(Transcript& t, const F& x) {
-  uint8_t b[8 * F::DEG];
+  uint8_t b[8 * F::LIMBS];
   elem_bytes(x, b);
   t.prover_bytes(b, sizeof(b));
 }
-// verifier_message<F>: per base coefficient squeeze 8 + 16 bytes, little-endian, reduced mod p.
+// Raw in-memory words of an element (host-internal storage, not an encoding).
+template <class F>
+inline void put_raw(std::vector<uint64_t>& dst, const F& x) {
+  const uint64_t* w = reinterpret_cast<const uint64_t*>(&x);
+  dst.insert(dst.end(), w, w + F::LIMBS);
+}
+template <class F>
+inline F get_raw(const uint64_t* w) {
+  F x;
+  memcpy(&x, w, sizeof(F));
+  return x;
+}
+
+// verifier_message<F>: per base coefficient squeeze (base bytes + 16) bytes, read as a
+// little-endian integer and reduced mod p.
 inline Gl gl_from_bytes_mod(const uint8_t* b, size_t n) {
   uint64_t acc = 0;
   const uint64_t two64 = GL_EPS;
@@ -226,25 +243,53 @@ inline Gl gl_from_bytes_mod(const uint8_t* b, size_t n) {
   }
   return Gl{acc};
 }
-template <class F>
-inline F from_coeffs(const uint64_t* c);
-template <>
-inline Gl from_coeffs<Gl>(const uint64_t* c) { return Gl{c[0]}; }
-template <>
-inline Gl2 from_coeffs<Gl2>(const uint64_t* c) { return Gl2{c[0], c[1]}; }
-template <>
-inline Gl3 from_coeffs<Gl3>(const uint64_t* c) { return Gl3{c[0], c[1], c[2]}; }
+template <class P>
+inline MontField<P> mont_from_bytes_mod(const uint8_t* b, size_t n) {
+  typedef MontField<P> M;
+  uint64_t l[M::N] = {0};
+  l[1] = 1;
+  const M two64 = M::from_canonical(l);
+  M acc = M::zero();
+  size_t words = (n + 7) / 8;
+  for (size_t w = words; w-- > 0;) {
+    uint64_t x = 0;
+    for (int i = 7; i >= 0; --i) {
+      size_t k = w * 8 + i;
+      x = (x << 8) | (k < n ? b[k] : 0);
+    }
+    uint64_t xl[M::N] = {0};
+    xl[0] = x;
+    acc = acc * two64 + M::from_canonical(xl);
+  }
+  return acc;
+}
 
 template <class F>
-inline F challenge(Transcript& t) {
-  uint64_t c[3];
-  uint8_t buf[24];
-  for (int d = 0; d < F::DEG; ++d) {
-    t.verifier_bytes(buf, 24);
-    c[d] = gl_from_bytes_mod(buf, 24).v;
+struct ChallengeCodec {
+  // Goldilocks family: DEG coefficients of 8 + 16 squeezed bytes each.
+  static F squeeze(Transcript& t) {
+    uint64_t c[F::LIMBS];
+    uint8_t buf[24];
+    for (int d = 0; d < F::DEG; ++d) {
+      t.verifier_bytes(buf, 24);
+      c[d] = gl_from_bytes_mod(buf, 24).v;
+    }
+    return Canon<F>::from(c);
   }
-  return from_coeffs<F>(c);
+};
+template <class P>
+struct ChallengeCodec<MontField<P>> {
+  static MontField<P> squeeze(Transcript& t) {
+    uint8_t buf[P::BYTES + 16];
+    t.verifier_bytes(buf, sizeof(buf));
+    return mont_from_bytes_mod<P>(buf, sizeof(buf));
+  }
+};
+template <class F>
+inline F challenge(Transcript& t) {
+  return ChallengeCodec<F>::squeeze(t);
 }
+
 template <class F>
 inline std::vector<F> geometric_challenge(Transcript& t, size_t count) {
   if (count == 0) return {};
@@ -279,23 +324,62 @@ inline std::vector<uint64_t> challenge_indices(Transcript& t, uint64_t num_leave
 }
 
 // ---------------------------------------------------------------------------------------------
-// Goldilocks roots of unity (cooley_tukey.rs:51-127): the engine order is 3 * 2^32 and
-// root(n) = 7^((p - 1) / n); extension engines use the same (lifted) roots.
+// Roots of unity (cooley_tukey.rs:51-127, NttEngine::new_from_fftfield): root(n) = g^((p-1)/n) for
+// n dividing the engine order; extension engines use the same (lifted) roots.
+//   Goldilocks g = 7, engine order 2^32 * 3   (fields.rs:85-91)
+//   Field192   g = 3, engine order 2^48       (two-adicity 48, no small subgroup)
+//   Field256   g = 5, engine order 2^28 * 3^2 (fields.rs:65-71)
 // ---------------------------------------------------------------------------------------------
-inline Gl gl_root(uint64_t n) {
-  if (n == 0) return Gl{1};
-  if ((3ull << 32) % n != 0) throw Error(-1, "Subgroup of requested order does not exist.");
-  return Gl{gl_pow(7, (GL_P - 1) / n)};
+template <class B>
+struct RootInfo;
+template <>
+struct RootInfo<Gl> {
+  static uint64_t engine_order() { return 3ull << 32; }
+  static Gl root(uint64_t n) { return Gl{gl_pow(7, (GL_P - 1) / n)}; }
+  static constexpr int TABLE_LOG = 32;  // device root tables hold powers of root(2^32)
+};
+template <class P>
+struct RootInfo<MontField<P>> {
+  typedef MontField<P> M;
+  static uint64_t engine_order() {
+    return P::TWO_ADICITY >= 63 ? 0 : (P::SMALL_ORDER << P::TWO_ADICITY);
+  }
+  static M root(uint64_t n) {
+    // (p - 1) / n by long division over the limbs, then g^quotient.
+    uint64_t q[M::N];
+    u128_t rem = 0;
+    for (int i = M::N - 1; i >= 0; --i) {
+      const uint64_t limb = i == 0 ? P::p(0) - 1 : P::p(i);
+      const u128_t cur = (rem << 64) | limb;
+      q[i] = (uint64_t)(cur / n);
+      rem = cur % n;
+    }
+    uint64_t g[M::N] = {0};
+    g[0] = P::GENERATOR;
+    return M::from_canonical(g).pow_limbs(q, M::N);
+  }
+  static constexpr int TABLE_LOG = P::TWO_ADICITY < 32 ? P::TWO_ADICITY : 32;
+};
+
+template <class B>
+inline B field_root(uint64_t n) {
+  if (n == 0) return B::one();
+  const uint64_t order = RootInfo<B>::engine_order();
+  if (order % n != 0) throw Error(-1, "Subgroup of requested order does not exist.");
+  return RootInfo<B>::root(n);
 }
+inline Gl gl_root(uint64_t n) { return field_root<Gl>(n); }
+
 // evaluation_points with the default (transpose-permuted) order (cooley_tukey.rs:375-402).
-inline std::vector<Gl> evaluation_points(uint64_t masked_len, uint64_t codeword_len, const std::vector<uint64_t>& idx) {
+template <class B>
+inline std::vector<B> evaluation_points(uint64_t masked_len, uint64_t codeword_len, const std::vector<uint64_t>& idx) {
   if (masked_len > codeword_len) throw Error(-1, "masked length exceeds codeword length");
   if (codeword_len == 0 || (codeword_len & (codeword_len - 1))) throw Error(-2, "codeword length must be a power of two");
   uint64_t C = 1;
   while (C < masked_len) C <<= 1;
   uint64_t K = codeword_len / C;
-  Gl g = gl_root(codeword_len);
-  std::vector<Gl> res;
+  B g = field_root<B>(codeword_len);
+  std::vector<B> res;
   for (uint64_t i : idx) {
     if (i >= codeword_len) throw Error(-1, "index out of range");
     uint64_t e = i / C + (i % C) * K;
@@ -418,9 +502,21 @@ struct Config {
   size_t size() const { return initial.vector_size; }
 };
 
+// log2 of the field size: modulus limbs accumulated as f64 (most significant first), times the
+// extension degree (fields.rs:10-30 field_size_bits).
 inline double field_bits_of(int field) {
-  double m = (double)GL_P;  // same rounding as the reference's limb-to-f64 conversion
-  int deg = field == 0 ? 1 : (field == 1 ? 2 : 3);
+  double m = 0.0;
+  int deg = 1;
+  if (field >= 0 && field <= 2) {
+    m = (double)GL_P;
+    deg = field + 1;
+  } else if (field == 4) {
+    for (int i = F192Params::N - 1; i >= 0; --i) m = m * 18446744073709551616.0 + (double)F192Params::p(i);
+  } else if (field == 5) {
+    for (int i = F256Params::N - 1; i >= 0; --i) m = m * 18446744073709551616.0 + (double)F256Params::p(i);
+  } else {
+    throw Error(-1, "unknown field id");
+  }
   return std::log2(m) * (double)deg;
 }
 
@@ -433,7 +529,7 @@ inline Pow make_pow(const uint8_t* id, double bits) {
 
 inline Config config_new(int field, size_t size, const Params& wp) {
   if (size == 0 || (size & (size - 1))) throw Error(-1, "Only powers of two size are supported at the moment.");
-  if (field < 0 || field > 2) throw Error(-2, "field not supported by the device prover");
+  if (field < 0 || field > 5 || field == 3) throw Error(-1, "unknown field id");
   if (engine_kind(wp.hash_id) < 0) throw Error(-1, "unknown hash engine id");
   if (wp.batch_size == 0) throw Error(-1, "batch_size must be positive");
   Config cfg;

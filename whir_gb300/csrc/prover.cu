@@ -48,8 +48,9 @@ enum ProfFamily { PF_ENCODE = 0, PF_MERKLE, PF_SUMCHECK, PF_EQ, PF_GEOMETRIC, PF
 struct whir_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
-  uint64_t* d_roots = nullptr;  // lo (2^16) then hi (2^16)
-  RootTab rt{};
+  // Root tables per base field (Goldilocks, Field192, Field256): lo (2^16) then hi entries.
+  uint64_t* d_roots[3] = {nullptr, nullptr, nullptr};
+  RootTab rts[3] = {};
   uint8_t* h_stage = nullptr;  // pinned staging for small transfers
   size_t h_stage_cap = 0;
   uint8_t* h_up = nullptr;  // pinned upload arena (see h2d)
@@ -193,20 +194,69 @@ void h2d(whir_ctx* ctx, void* dst, const void* src, size_t bytes) {
   ctx->up_off += (bytes + 255) & ~(size_t)255;
 }
 
+// Host arrays of canonical limbs <-> elements in their in-memory form.
 template <class T>
 std::vector<T> load_host(const uint64_t* p, size_t n) {
   std::vector<T> v(n);
   for (size_t i = 0; i < n; ++i) {
-    for (int d = 0; d < T::LIMBS; ++d)
-      if (p[i * T::LIMBS + d] >= GL_P) throw Error(WHIR_ERR_INVALID, "non-canonical field element");
-    v[i] = from_coeffs<T>(p + i * T::LIMBS);
+    if (!Canon<T>::ok(p + i * T::LIMBS)) throw Error(WHIR_ERR_INVALID, "non-canonical field element");
+    v[i] = Canon<T>::from(p + i * T::LIMBS);
   }
   return v;
 }
 template <class T>
 void store_host(const std::vector<T>& v, uint64_t* p) {
-  for (size_t i = 0; i < v.size(); ++i)
-    for (int d = 0; d < T::LIMBS; ++d) p[i * T::LIMBS + d] = v[i].coeff(d).v;
+  for (size_t i = 0; i < v.size(); ++i) Canon<T>::to(v[i], p + i * T::LIMBS);
+}
+template <class T>
+void store_one(const T& x, uint64_t* p) {
+  Canon<T>::to(x, p);
+}
+
+template <class B>
+struct RootSlot;
+template <>
+struct RootSlot<Gl> {
+  static constexpr int value = 0;
+};
+template <>
+struct RootSlot<F192> {
+  static constexpr int value = 1;
+};
+template <>
+struct RootSlot<F256> {
+  static constexpr int value = 2;
+};
+
+// Device root tables of base field B, built on first use in this context: w = root(2^L),
+// lo[i] = w^i (i < 2^16), hi[i] = w^(i 2^16) (i < 2^(L-16)), L = RootInfo<B>::TABLE_LOG.
+template <class B>
+const RootTab& root_tab(whir_ctx* ctx) {
+  constexpr int k = RootSlot<B>::value;
+  if (!ctx->d_roots[k]) {
+    const int L = RootInfo<B>::TABLE_LOG;
+    const size_t nlo = 1u << 16, nhi = (size_t)1 << (L - 16);
+    const B w = RootInfo<B>::root(1ull << L);
+    const B w16 = w.pow(1ull << 16);
+    std::vector<B> tab(nlo + nhi);
+    B x = B::one(), y = B::one();
+    for (size_t i = 0; i < nlo; ++i) {
+      tab[i] = x;
+      x = x * w;
+    }
+    for (size_t i = 0; i < nhi; ++i) {
+      tab[nlo + i] = y;
+      y = y * w16;
+    }
+    uint64_t* d = nullptr;
+    CU(cudaMalloc((void**)&d, tab.size() * sizeof(B)));
+    CU(cudaMemcpy(d, tab.data(), tab.size() * sizeof(B), cudaMemcpyHostToDevice));
+    ctx->d_roots[k] = d;
+    ctx->rts[k].lo = d;
+    ctx->rts[k].hi = d + nlo * (sizeof(B) / 8);
+    ctx->rts[k].log_order = L;
+  }
+  return ctx->rts[k];
 }
 
 }  // namespace
@@ -310,7 +360,7 @@ void encode_and_tree(whir_ctx* ctx, const F* d_msgs, size_t n_msgs, size_t msg_l
   {
     ProfScope prof(ctx, PF_ENCODE);
     CU(launch_encode<F>(plan, d_msgs, n_msgs, msg_len, reinterpret_cast<F*>(w.matrix.p), w.nodes.p, kind, scratch.p,
-                        ctx->rt, ctx->stream));
+                        root_tab<typename F::Base>(ctx), ctx->stream));
   }
   {
     ProfScope prof(ctx, PF_MERKLE);
@@ -346,15 +396,14 @@ std::unique_ptr<whir_witness> irs_commit(whir_ctx* ctx, const Irs& c, Transcript
   encode_and_tree<S>(ctx, d_vecs, c.num_cols, c.message_length(), c.codeword_length, kind, *w);
   ts.prover_bytes(w->root, 32);
   for (size_t i = 0; i < c.out_domain_samples; ++i) {
-    T pt = challenge<T>(ts);
-    for (int d = 0; d < T::LIMBS; ++d) w->ood_points.push_back(pt.coeff(d).v);
+    put_raw(w->ood_points, challenge<T>(ts));
   }
   for (size_t i = 0; i < c.out_domain_samples; ++i) {
-    T pt = from_coeffs<T>(&w->ood_points[i * T::LIMBS]);
+    T pt = get_raw<T>(&w->ood_points[i * T::LIMBS]);
     for (size_t v = 0; v < c.num_vectors; ++v) {
       T val = univariate_device<T, S>(ctx, d_vecs + v * c.vector_size, c.vector_size, pt);
       send_elem<T>(ts, val);
-      for (int d = 0; d < T::LIMBS; ++d) w->ood_matrix.push_back(val.coeff(d).v);
+      put_raw(w->ood_matrix, val);
     }
   }
   return w;
@@ -364,9 +413,9 @@ std::unique_ptr<whir_witness> irs_commit(whir_ctx* ctx, const Irs& c, Transcript
 // (points x (witnesses * num_cols)) in the witnesses' field F.
 template <class F>
 void irs_open(whir_ctx* ctx, const Irs& c, Transcript& ts, const std::vector<const whir_witness*>& ws,
-              std::vector<Gl>& points, std::vector<F>& rows, std::vector<uint64_t>* exps = nullptr) {
+              std::vector<typename F::Base>& points, std::vector<F>& rows, std::vector<uint64_t>* exps = nullptr) {
   std::vector<uint64_t> idx = challenge_indices(ts, c.codeword_length, c.in_domain_samples, c.dedup);
-  points = evaluation_points(c.masked_message_length(), c.codeword_length, idx);
+  points = evaluation_points<typename F::Base>(c.masked_message_length(), c.codeword_length, idx);
   if (exps) {
     // point = w_N^e with e = transpose_permute(index, K, C) (cooley_tukey.rs:391-399)
     uint64_t C = 1;
@@ -407,8 +456,8 @@ void irs_open(whir_ctx* ctx, const Irs& c, Transcript& ts, const std::vector<con
     uint64_t len = sub.size();
     for (int i = 0; i < 8; ++i) lb[i] = (uint8_t)(len >> (8 * i));
     ts.hint_bytes(lb, 8);
-    std::vector<uint8_t> eb(sub.size() * 8 * F::DEG);
-    for (size_t i = 0; i < sub.size(); ++i) elem_bytes(sub[i], eb.data() + i * 8 * F::DEG);
+    std::vector<uint8_t> eb(sub.size() * 8 * F::LIMBS);
+    for (size_t i = 0; i < sub.size(); ++i) elem_bytes(sub[i], eb.data() + i * 8 * F::LIMBS);
     ts.hint_bytes(eb.data(), eb.size());
     ts.hint_bytes(sib.data(), sib.size());
     for (size_t pi = 0; pi < q; ++pi)
@@ -546,7 +595,8 @@ void accumulate_in_domain(whir_ctx* ctx, T* cov, size_t len, const std::vector<T
     DBuf<uint64_t> de(ctx, exps.size());
     h2d(ctx, ds.p, scalars.data(), scalars.size() * sizeof(T));
     h2d(ctx, de.p, exps.data(), exps.size() * sizeof(uint64_t));
-    CU(launch_geometric_roots<T>(cov, len, ds.p, de.p, scalars.size(), logN, ctx->rt, ctx->stream));
+    CU(launch_geometric_roots<T>(cov, len, ds.p, de.p, scalars.size(), logN, root_tab<typename T::Base>(ctx),
+                                 ctx->stream));
     return;
   }
   // Combine repeated query positions (indices are sampled with replacement).
@@ -574,7 +624,8 @@ void accumulate_in_domain(whir_ctx* ctx, T* cov, size_t len, const std::vector<T
   int rc = plan_encode(1, N, N, sizeof(T), &plan);
   if (rc) throw Error(rc, "NTT shape unsupported on the device");
   DBuf<T> scratch(ctx, plan.scratch_elems);
-  CU(launch_encode<T>(plan, dense.p, 1, N, out.p, nullptr, HASH_BLAKE3, scratch.p, ctx->rt, ctx->stream));
+  CU(launch_encode<T>(plan, dense.p, 1, N, out.p, nullptr, HASH_BLAKE3, scratch.p, root_tab<typename T::Base>(ctx),
+                      ctx->stream));
   CU(launch_add<T>(cov, out.p, len, ctx->stream));
 }
 
@@ -623,10 +674,10 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
     const size_t wn = w->num_vectors(T::LIMBS);
     const size_t np = w->ood_points.size() / T::LIMBS;
     for (size_t oi = 0; oi < np; ++oi) {
-      const T pt = from_coeffs<T>(&w->ood_points[oi * T::LIMBS]);
+      const T pt = get_raw<T>(&w->ood_points[oi * T::LIMBS]);
       for (size_t j = 0; j < nv; ++j) {
         if (j >= voff && j < voff + wn) {
-          oods_matrix.push_back(from_coeffs<T>(&w->ood_matrix[(oi * wn + (j - voff)) * T::LIMBS]));
+          oods_matrix.push_back(get_raw<T>(&w->ood_matrix[(oi * wn + (j - voff)) * T::LIMBS]));
         } else {
           T e = univariate_device<T, S>(ctx, d_vectors + j * n, n, pt);
           send_elem<T>(ts, e);
@@ -741,7 +792,7 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
     if (len != rc.irs.vector_size) throw Error(WHIR_ERR_INTERNAL, "round vector size mismatch");
     std::unique_ptr<whir_witness> nw = irs_commit<T, T>(ctx, rc.irs, ts, a.p, cfg.field);
     pow_prove(ctx, rc.pow, ts);
-    std::vector<Gl> pts;
+    std::vector<typename T::Base> pts;
     std::vector<T> in_rows;
     std::vector<uint64_t> exps;
     const size_t prev_N = prev ? cfg.rounds[ri - 1].irs.codeword_length : cfg.initial.codeword_length;
@@ -758,10 +809,10 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
     std::vector<T> stir_evals;
     const size_t nood = nw->ood_points.size() / T::LIMBS;
     for (size_t o = 0; o < nood; ++o) {
-      stir_points.push_back(from_coeffs<T>(&nw->ood_points[o * T::LIMBS]));
-      stir_evals.push_back(from_coeffs<T>(&nw->ood_matrix[o * T::LIMBS]));
+      stir_points.push_back(get_raw<T>(&nw->ood_points[o * T::LIMBS]));
+      stir_evals.push_back(get_raw<T>(&nw->ood_matrix[o * T::LIMBS]));
     }
-    for (const Gl& p : pts) stir_points.push_back(T::from_base(p));
+    for (const auto& p : pts) stir_points.push_back(T::from_base(p));
     {
       std::vector<T> eqw = eq_weights_host(folding);
       std::vector<T> wts;
@@ -799,7 +850,7 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
   for (const T& x : fin) send_elem<T>(ts, x);
   pow_prove(ctx, cfg.final_pow, ts);
   {
-    std::vector<Gl> pts;
+    std::vector<typename T::Base> pts;
     if (!prev) {
       std::vector<S> rows;
       irs_open<S>(ctx, cfg.initial, ts, witnesses, pts, rows);
@@ -815,21 +866,66 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
   CU(cudaStreamSynchronize(ctx->stream));
 }
 
-// Copies host vectors to the device when needed; returns a device pointer valid for the call.
-// Small operator inputs are checked for canonical form on the host; the polynomial vectors of
-// commit/prove are taken as given (like the reference's ark-ff elements, they must be canonical).
+// Device copy, in the in-memory form of S, of a read-only input array of canonical limbs (host
+// memory, or device memory with WHIR_DEVICE_PTRS); returns a device pointer valid for the call.
+// Canonical device inputs of the Goldilocks family are used in place. Small operator inputs are
+// checked for canonical form on the host; the polynomial vectors of commit/prove are taken as given
+// (like the reference's ark-ff elements, they must be canonical).
 template <class S>
 const S* device_vectors(whir_ctx* ctx, const uint64_t* vectors, size_t count, uint32_t flags, DBuf<S>& holder,
                         bool validate = true) {
-  if (flags & WHIR_DEVICE_PTRS) return reinterpret_cast<const S*>(vectors);
-  if (validate)
-    for (size_t i = 0; i < count * S::LIMBS; ++i)
-      if (vectors[i] >= GL_P) throw Error(WHIR_ERR_INVALID, "non-canonical field element in input vector");
+  const bool dev = (flags & WHIR_DEVICE_PTRS) != 0;
+  if (dev && Canon<S>::IDENTITY) return reinterpret_cast<const S*>(vectors);
+  if (validate && !dev)
+    for (size_t i = 0; i < count; ++i)
+      if (!Canon<S>::ok(vectors + i * S::LIMBS))
+        throw Error(WHIR_ERR_INVALID, "non-canonical field element in input vector");
   holder = DBuf<S>(ctx, count);
-  ctx->h2d_bytes += count * sizeof(S);
-  CU(cudaMemcpyAsync(holder.p, vectors, count * sizeof(S), cudaMemcpyHostToDevice, ctx->stream));
+  if (!count) return holder.p;
+  if (!dev) ctx->h2d_bytes += count * sizeof(S);
+  CU(cudaMemcpyAsync(holder.p, vectors, count * sizeof(S), dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CU(launch_to_internal<S>(holder.p, count, ctx->stream));
   return holder.p;
 }
+
+// An in/out array of canonical limbs for the operator entry points: with WHIR_DEVICE_PTRS the
+// caller's device buffer is converted to the in-memory form in place (and back by finish());
+// otherwise a device copy is made and finish() copies `back` elements of the result to the host.
+template <class T>
+struct InOut {
+  whir_ctx* ctx;
+  uint64_t* user;
+  size_t n;
+  bool dev;
+  DBuf<T> own;
+  T* p = nullptr;
+  InOut(whir_ctx* c, uint64_t* u, size_t count, uint32_t flags) : ctx(c), user(u), n(count) {
+    dev = (flags & WHIR_DEVICE_PTRS) != 0;
+    if (dev) {
+      p = reinterpret_cast<T*>(user);
+    } else {
+      for (size_t i = 0; i < n; ++i)
+        if (!Canon<T>::ok(user + i * T::LIMBS)) throw Error(WHIR_ERR_INVALID, "non-canonical field element");
+      own = DBuf<T>(ctx, n);
+      p = own.p;
+      if (n) {
+        ctx->h2d_bytes += n * sizeof(T);
+        CU(cudaMemcpyAsync(p, user, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+      }
+    }
+    CU(launch_to_internal<T>(p, n, ctx->stream));
+  }
+  // Converts the whole array back to canonical limbs and copies the first `back` elements home.
+  void finish(size_t back) {
+    CU(launch_to_canonical<T>(p, n, ctx->stream));
+    if (!dev && back) {
+      ctx->d2h_bytes += back * sizeof(T);
+      CU(cudaMemcpyAsync(user, p, back * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    CU(cudaStreamSynchronize(ctx->stream));
+  }
+};
 
 template <class Fn>
 int guarded(Fn&& fn) {
@@ -844,14 +940,6 @@ int guarded(Fn&& fn) {
   }
 }
 
-int target_limbs(int field) {
-  switch (field) {
-    case WHIR_GOLDILOCKS1: return 1;
-    case WHIR_GOLDILOCKS2: return 2;
-    case WHIR_GOLDILOCKS3: return 3;
-    default: return -1;
-  }
-}
 
 // Calls f.template operator()<S, T>() for the embedding id.
 template <class Fn>
@@ -860,8 +948,8 @@ int with_embedding(int field, Fn&& f) {
     case WHIR_GOLDILOCKS1: return f.template operator()<Gl, Gl>();
     case WHIR_GOLDILOCKS2: return f.template operator()<Gl, Gl2>();
     case WHIR_GOLDILOCKS3: return f.template operator()<Gl, Gl3>();
-    case WHIR_FIELD192:
-    case WHIR_FIELD256: throw Error(WHIR_ERR_UNSUPPORTED, "Field192/Field256 are not implemented on the device");
+    case WHIR_FIELD192: return f.template operator()<F192, F192>();
+    case WHIR_FIELD256: return f.template operator()<F256, F256>();
     default: throw Error(WHIR_ERR_INVALID, "unknown field id");
   }
 }
@@ -872,8 +960,8 @@ int with_field(int field, Fn&& f) {
     case WHIR_GOLDILOCKS1: return f.template operator()<Gl>();
     case WHIR_GOLDILOCKS2: return f.template operator()<Gl2>();
     case WHIR_GOLDILOCKS3: return f.template operator()<Gl3>();
-    case WHIR_FIELD192:
-    case WHIR_FIELD256: throw Error(WHIR_ERR_UNSUPPORTED, "Field192/Field256 are not implemented on the device");
+    case WHIR_FIELD192: return f.template operator()<F192>();
+    case WHIR_FIELD256: return f.template operator()<F256>();
     default: throw Error(WHIR_ERR_INVALID, "unknown field id");
   }
 }
@@ -910,21 +998,7 @@ int whir_ctx_create(int device, whir_ctx** out) {
     CU(cudaDeviceGetDefaultMemPool(&pool, device));
     uint64_t thr = UINT64_MAX;
     CU(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
-    // Root tables: w = 7^((p-1)/2^32), lo[i] = w^i, hi[i] = w^(i 2^16).
-    std::vector<uint64_t> tab(2 << 16);
-    const uint64_t w = gl_pow(7, (GL_P - 1) >> 32);
-    const uint64_t w16 = gl_pow(w, 1ull << 16);
-    uint64_t x = 1, y = 1;
-    for (size_t i = 0; i < (1u << 16); ++i) {
-      tab[i] = x;
-      tab[(1u << 16) + i] = y;
-      x = gl_mul(x, w);
-      y = gl_mul(y, w16);
-    }
-    CU(cudaMalloc((void**)&ctx->d_roots, tab.size() * sizeof(uint64_t)));
-    CU(cudaMemcpy(ctx->d_roots, tab.data(), tab.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
-    ctx->rt.lo = ctx->d_roots;
-    ctx->rt.hi = ctx->d_roots + (1u << 16);
+    root_tab<Gl>(ctx.get());  // the other fields' tables are built on first use
     CU(cudaMalloc((void**)&ctx->d_pow, 2 * sizeof(unsigned long long)));
     stage_reserve(ctx.get(), 1 << 20);
     ctx->up_cap = 8 << 20;
@@ -944,7 +1018,8 @@ int whir_ctx_destroy(whir_ctx* ctx) {
     cudaEventDestroy(p.second.second);
   }
   for (auto e : ctx->event_pool) cudaEventDestroy(e);
-  if (ctx->d_roots) cudaFree(ctx->d_roots);
+  for (uint64_t* r : ctx->d_roots)
+    if (r) cudaFree(r);
   if (ctx->d_pow) cudaFree(ctx->d_pow);
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
   if (ctx->h_up) cudaFreeHost(ctx->h_up);
@@ -1032,8 +1107,6 @@ int whir_memcpy_d2h(whir_ctx* ctx, void* dst, const void* src, size_t bytes) {
 int whir_config_new(int field, const whir_params* p, uint64_t size, whir_config** out) {
   return guarded([&] {
     if (!p || !out) throw Error(WHIR_ERR_INVALID, "null argument");
-    if (field == WHIR_FIELD192 || field == WHIR_FIELD256)
-      throw Error(WHIR_ERR_UNSUPPORTED, "Field192/Field256 are not implemented on the device");
     Params wp;
     wp.unique_decoding = p->unique_decoding != 0;
     wp.starting_log_inv_rate = p->starting_log_inv_rate;
@@ -1139,20 +1212,18 @@ int whir_commit(whir_ctx* ctx, const whir_config* cfg, whir_prover_state* ps, co
     const Config& c = cfg->cfg;
     return with_embedding(c.field, [&]<class S, class T>() {
       const size_t count = c.initial.num_vectors * c.size();
-      DBuf<uint64_t> copy;
-      const S* d = reinterpret_cast<const S*>(vectors);
-      if (!(flags & WHIR_DEVICE_PTRS)) {
-        copy = DBuf<uint64_t>(ctx, count * S::LIMBS);
-        ctx->h2d_bytes += count * sizeof(S);
-        CU(cudaMemcpyAsync(copy.p, vectors, count * sizeof(S), cudaMemcpyHostToDevice, ctx->stream));
-        d = reinterpret_cast<const S*>(copy.p);
-      }
+      DBuf<S> copy;
+      const S* d = device_vectors<S>(ctx, vectors, count, flags, copy, false);
       auto w = irs_commit<S, T>(ctx, c.initial, ps->ts, d, c.field);
       CU(cudaStreamSynchronize(ctx->stream));
       if (!(flags & WHIR_DEVICE_PTRS)) {
         // Keep the device copy: prove() given the same host buffer reuses it instead of copying again.
         w->host_src = vectors;
-        w->vectors = std::move(copy);
+        w->vectors = DBuf<uint64_t>();
+        w->vectors.ctx = ctx;
+        w->vectors.p = reinterpret_cast<uint64_t*>(copy.p);
+        w->vectors.n = count * S::LIMBS;
+        copy.p = nullptr;
       }
       *out = w.release();
       return 0;
@@ -1229,7 +1300,9 @@ int whir_rs_interleaved_encode(whir_ctx* ctx, int field, const uint64_t* msgs, s
       int rc = plan_encode(n_msgs, msg_len, codeword_len, sizeof(F), &plan);
       if (rc) throw Error(rc, "encode shape unsupported on the device");
       DBuf<F> scratch(ctx, plan.scratch_elems);
-      CU(launch_encode<F>(plan, d_in, n_msgs, msg_len, d_out, nullptr, HASH_BLAKE3, scratch.p, ctx->rt, ctx->stream));
+      CU(launch_encode<F>(plan, d_in, n_msgs, msg_len, d_out, nullptr, HASH_BLAKE3, scratch.p,
+                          root_tab<typename F::Base>(ctx), ctx->stream));
+      CU(launch_to_canonical<F>(d_out, codeword_len * n_msgs, ctx->stream));
       if (!(flags & WHIR_DEVICE_PTRS))
         CU(cudaMemcpyAsync(out, d_out, codeword_len * n_msgs * sizeof(F), cudaMemcpyDeviceToHost, ctx->stream));
       CU(cudaStreamSynchronize(ctx->stream));
@@ -1241,16 +1314,13 @@ int whir_rs_interleaved_encode(whir_ctx* ctx, int field, const uint64_t* msgs, s
 int whir_rs_evaluation_points(int field, size_t masked_len, size_t codeword_len, const uint64_t* indices, size_t n,
                               uint64_t* out) {
   return guarded([&] {
-    int L = target_limbs(field);
-    if (L < 0) throw Error(field == WHIR_FIELD192 || field == WHIR_FIELD256 ? WHIR_ERR_UNSUPPORTED : WHIR_ERR_INVALID,
-                           "field not supported");
-    std::vector<uint64_t> idx(indices, indices + n);
-    std::vector<Gl> pts = evaluation_points(masked_len, codeword_len, idx);
-    for (size_t i = 0; i < n; ++i) {
-      out[i * L] = pts[i].v;
-      for (int d = 1; d < L; ++d) out[i * L + d] = 0;
-    }
-    return 0;
+    return with_field(field, [&]<class F>() {
+      typedef typename F::Base B;
+      std::vector<uint64_t> idx(indices, indices + n);
+      std::vector<B> pts = evaluation_points<B>(masked_len, codeword_len, idx);
+      for (size_t i = 0; i < n; ++i) store_one<F>(F::from_base(pts[i]), out + i * F::LIMBS);
+      return 0;
+    });
   });
 }
 
@@ -1308,7 +1378,8 @@ int whir_sumcheck_polynomial(whir_ctx* ctx, int field, const uint64_t* a, const 
     if (n && (n & (n - 1))) throw Error(WHIR_ERR_UNSUPPORTED, "length must be a power of two on the device");
     return with_field(field, [&]<class T>() {
       if (n == 0) {
-        for (int d = 0; d < T::LIMBS; ++d) c0[d] = c2[d] = 0;
+        store_one<T>(T::zero(), c0);
+        store_one<T>(T::zero(), c2);
         return 0;
       }
       DBuf<T> ha, hb;
@@ -1320,10 +1391,8 @@ int whir_sumcheck_polynomial(whir_ctx* ctx, int field, const uint64_t* a, const 
       CU(launch_reduce_pairs<T>(parts.p, np, res.p, ctx->stream));
       T r[2];
       d2h(ctx, r, res.p, sizeof(r));
-      for (int d = 0; d < T::LIMBS; ++d) {
-        c0[d] = r[0].coeff(d).v;
-        c2[d] = r[1].coeff(d).v;
-      }
+      store_one<T>(r[0], c0);
+      store_one<T>(r[1], c2);
       return 0;
     });
   });
@@ -1336,11 +1405,9 @@ int whir_fold(whir_ctx* ctx, int field, uint64_t* v, size_t n, const uint64_t* w
     return with_field(field, [&]<class T>() {
       T w = load_host<T>(weight, 1)[0];
       if (n <= 1) return 0;
-      DBuf<T> hv;
-      T* dv = (flags & WHIR_DEVICE_PTRS) ? reinterpret_cast<T*>(v) : const_cast<T*>(device_vectors<T>(ctx, v, n, flags, hv));
-      CU(launch_fold<T>(dv, n, w, ctx->stream));
-      if (!(flags & WHIR_DEVICE_PTRS)) CU(cudaMemcpyAsync(v, dv, (n / 2) * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
-      CU(cudaStreamSynchronize(ctx->stream));
+      InOut<T> dv(ctx, v, n, flags);
+      CU(launch_fold<T>(dv.p, n, w, ctx->stream));
+      dv.finish(n / 2);
       return 0;
     });
   });
@@ -1353,9 +1420,9 @@ int whir_eval_eq(whir_ctx* ctx, int field, uint64_t* acc, const uint64_t* point,
     return with_field(field, [&]<class T>() {
       T s = load_host<T>(scalar, 1)[0];
       const size_t n = 1ull << nvars;
-      DBuf<T> hacc, hpt;
-      T* dacc = (flags & WHIR_DEVICE_PTRS) ? reinterpret_cast<T*>(acc)
-                                           : const_cast<T*>(device_vectors<T>(ctx, acc, n, flags, hacc));
+      DBuf<T> hpt;
+      InOut<T> io(ctx, acc, n, flags);
+      T* dacc = io.p;
       const T* dpt = nvars ? device_vectors<T>(ctx, point, nvars, flags, hpt) : nullptr;
       DBuf<T> tables(ctx, (2ull << ((nvars + 1) / 2)) + 2);
       if (nvars == 0) {
@@ -1370,8 +1437,7 @@ int whir_eval_eq(whir_ctx* ctx, int field, uint64_t* acc, const uint64_t* point,
       } else {
         CU(launch_eval_eq<T>(dacc, dpt, (int)nvars, s, tables.p, ctx->stream));
       }
-      if (!(flags & WHIR_DEVICE_PTRS)) CU(cudaMemcpyAsync(acc, dacc, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
-      CU(cudaStreamSynchronize(ctx->stream));
+      io.finish(n);
       return 0;
     });
   });
@@ -1383,14 +1449,12 @@ int whir_geometric_accumulate(whir_ctx* ctx, int field, uint64_t* acc, size_t n,
     check_ctx(ctx);
     return with_field(field, [&]<class T>() {
       if (n == 0 || m == 0) return 0;
-      DBuf<T> hacc, hs, hp;
-      T* dacc = (flags & WHIR_DEVICE_PTRS) ? reinterpret_cast<T*>(acc)
-                                           : const_cast<T*>(device_vectors<T>(ctx, acc, n, flags, hacc));
+      DBuf<T> hs, hp;
+      InOut<T> io(ctx, acc, n, flags);
       const T* ds = device_vectors<T>(ctx, scalars, m, flags, hs);
       const T* dp = device_vectors<T>(ctx, points, m, flags, hp);
-      CU(launch_geometric_accumulate<T>(dacc, n, ds, dp, m, ctx->stream));
-      if (!(flags & WHIR_DEVICE_PTRS)) CU(cudaMemcpyAsync(acc, dacc, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
-      CU(cudaStreamSynchronize(ctx->stream));
+      CU(launch_geometric_accumulate<T>(io.p, n, ds, dp, m, ctx->stream));
+      io.finish(n);
       return 0;
     });
   });
@@ -1408,7 +1472,7 @@ int whir_univariate_evaluate(whir_ctx* ctx, int field, const uint64_t* coeffs, s
         const S* dc = device_vectors<S>(ctx, coeffs, n, flags, hc);
         r = univariate_device<T, S>(ctx, dc, n, x);
       }
-      for (int d = 0; d < T::LIMBS; ++d) out[d] = r.coeff(d).v;
+      store_one<T>(r, out);
       return 0;
     });
   });
@@ -1436,7 +1500,7 @@ int whir_multilinear_evaluate(whir_ctx* ctx, int field, const uint64_t* coeffs, 
         CU(launch_reduce_singles<T>(parts.p, np, res.p, ctx->stream));
         d2h(ctx, &r, res.p, sizeof(T));
       }
-      for (int d = 0; d < T::LIMBS; ++d) out[d] = r.coeff(d).v;
+      store_one<T>(r, out);
       return 0;
     });
   });

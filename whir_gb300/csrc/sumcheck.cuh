@@ -1,0 +1,610 @@
+// Sumcheck-side kernel templates of the WHIR prover path (instantiated in sumcheck.cu for the
+// Goldilocks family and in sumcheck_mont.cu for Field192/Field256):
+//   sumcheck round polynomial (c0, c2) and the in-place fold, fused as fold-then-compute
+//     (reference src/algebra/sumcheck.rs:12-111, protocols/sumcheck.rs:104-155)
+//   eq-weight accumulation (multilinear.rs:170-190, linear_form/multilinear_extension.rs:38-40)
+//   geometric accumulation of STIR / OOD constraints (algebra/mod.rs:154-177)
+//   base -> extension lift and vector RLC (algebra/mod.rs:51-98)
+//   univariate (Horner) evaluation for out-of-domain samples (algebra/mod.rs:105-129)
+// Every value is an exact field element, so the reduction order inside the kernels does not
+// change any output bit relative to the reference's rayon split order.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "field.cuh"
+#include "kernels.hpp"
+#include "roots.cuh"
+
+namespace whir {
+
+static constexpr int SC_THREADS = 256;
+static constexpr size_t SC_MAX_BLOCKS = 152 * 8;
+
+template <class T>
+__device__ __forceinline__ T shfl_down_t(const T& x, int d) {
+  T r;
+  const uint64_t* src = reinterpret_cast<const uint64_t*>(&x);
+  uint64_t* dst = reinterpret_cast<uint64_t*>(&r);
+#pragma unroll
+  for (int i = 0; i < (int)(sizeof(T) / 8); ++i) dst[i] = __shfl_down_sync(0xffffffffu, src[i], d);
+  return r;
+}
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T x) {
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) x = x + shfl_down_t(x, d);
+  return x;
+}
+
+// Block-wide sum; the result is valid in thread 0.
+template <class T>
+__device__ T block_sum(T x) {
+  __shared__ T part[32];
+  x = warp_sum(x);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) part[warp] = x;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  x = (threadIdx.x < nw) ? part[threadIdx.x] : T::zero();
+  if (warp == 0) x = warp_sum(x);
+  __syncthreads();
+  return x;
+}
+
+template <class T>
+__device__ __forceinline__ T ldcg_t(const T* p) {
+  T r;
+  const unsigned long long* s = reinterpret_cast<const unsigned long long*>(p);
+  unsigned long long* d = reinterpret_cast<unsigned long long*>(&r);
+#pragma unroll
+  for (int i = 0; i < (int)(sizeof(T) / 8); ++i) d[i] = __ldcg(s + i);
+  return r;
+}
+
+// Stores this block's (c0, c2) partial. With a counter, the last block to finish also sums all
+// partials into out[0..2) and re-arms the counter, so one launch yields the round message.
+template <class T>
+__device__ void finish_pairs(T acc0, T acc2, T* partials, T* out, unsigned int* counter) {
+  __shared__ bool am_last;
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = acc0;
+    partials[2 * blockIdx.x + 1] = acc2;
+    am_last = false;
+    if (counter) {
+      __threadfence();
+      am_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+  }
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  T s0 = T::zero(), s2 = T::zero();
+  for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
+    s0 += ldcg_t(partials + 2 * i);
+    s2 += ldcg_t(partials + 2 * i + 1);
+  }
+  s0 = block_sum(s0);
+  s2 = block_sum(s2);
+  if (threadIdx.x == 0) {
+    out[0] = s0;
+    out[1] = s2;
+    *counter = 0;
+  }
+}
+
+
+template <class T>
+__global__ void __launch_bounds__(SC_THREADS) sc_compute_kernel(const T* a, const T* b, uint64_t n, T* partials,
+                                                                 T* out, unsigned int* counter) {
+  T acc0 = T::zero(), acc2 = T::zero();
+  if (n == 1) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) acc0 = a[0] * b[0];
+  } else {
+    const uint64_t h = n >> 1;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < h; i += (uint64_t)gridDim.x * blockDim.x) {
+      const T a0 = a[i], a1 = a[i + h], b0 = b[i], b1 = b[i + h];
+      acc0 += a0 * b0;
+      acc2 += (a1 - a0) * (b1 - b0);
+    }
+  }
+  acc0 = block_sum(acc0);
+  acc2 = block_sum(acc2);
+  finish_pairs(acc0, acc2, partials, out, counter);
+}
+
+template <class T>
+__global__ void __launch_bounds__(SC_THREADS) sc_fold_compute_kernel(T* a, T* b, uint64_t n, T r, T* partials,
+                                                                      T* out, unsigned int* counter) {
+  T acc0 = T::zero(), acc2 = T::zero();
+  if (n <= 2) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      if (n == 2) {
+        const T fa = a[0] + (a[1] - a[0]) * r, fb = b[0] + (b[1] - b[0]) * r;
+        a[0] = fa;
+        b[0] = fb;
+        acc0 = fa * fb;
+      } else if (n == 1) {
+        acc0 = a[0] * b[0];
+      }
+    }
+  } else {
+    const uint64_t q = n >> 2, h = n >> 1;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < q; i += (uint64_t)gridDim.x * blockDim.x) {
+      const T a0 = a[i], a1 = a[i + q], a2 = a[i + h], a3 = a[i + h + q];
+      const T b0 = b[i], b1 = b[i + q], b2 = b[i + h], b3 = b[i + h + q];
+      const T fa0 = a0 + (a2 - a0) * r, fa1 = a1 + (a3 - a1) * r;
+      const T fb0 = b0 + (b2 - b0) * r, fb1 = b1 + (b3 - b1) * r;
+      a[i] = fa0;
+      a[i + q] = fa1;
+      b[i] = fb0;
+      b[i + q] = fb1;
+      acc0 += fa0 * fb0;
+      acc2 += (fa1 - fa0) * (fb1 - fb0);
+    }
+  }
+  acc0 = block_sum(acc0);
+  acc2 = block_sum(acc2);
+  finish_pairs(acc0, acc2, partials, out, counter);
+}
+
+template <class T>
+__global__ void __launch_bounds__(SC_THREADS) sc_fold_kernel(T* v, uint64_t n, T r) {
+  const uint64_t h = n >> 1;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < h; i += (uint64_t)gridDim.x * blockDim.x) {
+    const T lo = v[i], hi = v[i + h];
+    v[i] = lo + (hi - lo) * r;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(SC_THREADS) reduce_pairs_kernel(const T* partials, uint64_t nparts, T* out) {
+  T s0 = T::zero(), s2 = T::zero();
+  for (uint64_t i = threadIdx.x; i < nparts; i += blockDim.x) {
+    s0 += partials[2 * i];
+    s2 += partials[2 * i + 1];
+  }
+  s0 = block_sum(s0);
+  s2 = block_sum(s2);
+  if (threadIdx.x == 0) {
+    out[0] = s0;
+    out[1] = s2;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(SC_THREADS) reduce_singles_kernel(const T* partials, uint64_t nparts, T* out) {
+  T s = T::zero();
+  for (uint64_t i = threadIdx.x; i < nparts; i += blockDim.x) s += partials[i];
+  s = block_sum(s);
+  if (threadIdx.x == 0) out[0] = s;
+}
+
+template <class T>
+cudaError_t launch_sumcheck_compute(const T* a, const T* b, size_t n, T* partials, size_t* nparts, cudaStream_t s,
+                                    T* out, unsigned int* counter) {
+  size_t g = sumcheck_partials(n);
+  sc_compute_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(a, b, n, partials, out, counter);
+  note_launch();
+  *nparts = g;
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_fold_compute(T* a, T* b, size_t n, T r, T* partials, size_t* nparts, cudaStream_t s, T* out,
+                                unsigned int* counter) {
+  size_t g = sumcheck_partials(n);
+  sc_fold_compute_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(a, b, n, r, partials, out, counter);
+  note_launch();
+  *nparts = g;
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_fold(T* v, size_t n, T r, cudaStream_t s) {
+  if (n <= 1) return cudaSuccess;
+  size_t g = std::min(SC_MAX_BLOCKS, (n / 2 + SC_THREADS - 1) / SC_THREADS);
+  sc_fold_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(v, n, r);
+  note_launch();
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_reduce_pairs(const T* partials, size_t nparts, T* out, cudaStream_t s) {
+  reduce_pairs_kernel<T><<<1, SC_THREADS, 0, s>>>(partials, nparts, out);
+  note_launch();
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_reduce_singles(const T* partials, size_t nparts, T* out, cudaStream_t s) {
+  reduce_singles_kernel<T><<<1, SC_THREADS, 0, s>>>(partials, nparts, out);
+  note_launch();
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// eq weights: acc[i] += hi[i >> l] * lo[i & (2^l - 1)], hi = scalar * eq(point[0..h)),
+// lo = eq(point[h..nv)).
+// ---------------------------------------------------------------------------------------------
+template <class T>
+__global__ void eq_table_kernel(const T* point, int off, int cnt, T scalar, T* table) {
+  const uint64_t size = 1ull << cnt;
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < size; e += (uint64_t)gridDim.x * blockDim.x) {
+    T v = scalar;
+    for (int k = 0; k < cnt; ++k) {
+      const T x = point[off + k];
+      const bool bit = (e >> (cnt - 1 - k)) & 1;
+      v = v * (bit ? x : (T::one() - x));
+    }
+    table[e] = v;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(SC_THREADS) eq_accumulate_kernel(T* acc, uint64_t n, const T* hi, const T* lo, int l) {
+  const uint64_t mask = (1ull << l) - 1;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    acc[i] += hi[i >> l] * lo[i & mask];
+}
+
+template <class T>
+cudaError_t launch_eval_eq(T* acc, const T* point, int nv, T scalar, T* tables, cudaStream_t s) {
+  const int h = nv / 2, l = nv - h;
+  T* hi = tables;
+  T* lo = tables + (1ull << h);
+  eq_table_kernel<T><<<(unsigned)std::max<size_t>(1, ((1ull << h) + 255) / 256), 256, 0, s>>>(point, 0, h, scalar, hi);
+  note_launch();
+  eq_table_kernel<T><<<(unsigned)std::max<size_t>(1, ((1ull << l) + 255) / 256), 256, 0, s>>>(point, h, l, T::one(), lo);
+  note_launch();
+  const uint64_t n = 1ull << nv;
+  size_t g = std::min<size_t>(SC_MAX_BLOCKS * 2, (n + SC_THREADS - 1) / SC_THREADS);
+  eq_accumulate_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(acc, n, hi, lo, l);
+  note_launch();
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Geometric accumulation: acc[i] += sum_j s_j x_j^i. CTA covers GA_E * blockDim consecutive
+// indices; thread t handles i = base + t + u * blockDim (u < GA_E) so every access is coalesced.
+// Per point: p = s_j x_j^(base + t) then p *= x_j^blockDim per step.
+// ---------------------------------------------------------------------------------------------
+static constexpr int GA_E = 16;
+static constexpr int GA_THREADS = 256;
+static constexpr int GA_CHUNK = 64;  // points staged in shared memory at a time
+
+template <class T>
+__global__ void __launch_bounds__(GA_THREADS) geometric_kernel(T* acc, uint64_t n, const T* scalars, const T* points,
+                                                               uint64_t m) {
+  __shared__ T sA[GA_CHUNK];  // s_j * x_j^base
+  __shared__ T sB[GA_CHUNK];  // x_j^blockDim
+  __shared__ T sX[GA_CHUNK];  // x_j
+  const uint64_t base = (uint64_t)blockIdx.x * GA_THREADS * GA_E;
+  T accu[GA_E];
+#pragma unroll
+  for (int u = 0; u < GA_E; ++u) accu[u] = T::zero();
+  for (uint64_t j0 = 0; j0 < m; j0 += GA_CHUNK) {
+    const int cnt = (int)std::min<uint64_t>(GA_CHUNK, m - j0);
+    __syncthreads();
+    if (threadIdx.x < cnt) {
+      const T x = points[j0 + threadIdx.x];
+      sX[threadIdx.x] = x;
+      sA[threadIdx.x] = scalars[j0 + threadIdx.x] * x.pow(base);
+      sB[threadIdx.x] = x.pow(GA_THREADS);
+    }
+    __syncthreads();
+    for (int j = 0; j < cnt; ++j) {
+      T p = sA[j] * sX[j].pow(threadIdx.x);
+      const T stepv = sB[j];
+#pragma unroll
+      for (int u = 0; u < GA_E; ++u) {
+        accu[u] += p;
+        p = p * stepv;
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < GA_E; ++u) {
+    const uint64_t i = base + threadIdx.x + (uint64_t)u * GA_THREADS;
+    if (i < n) acc[i] += accu[u];
+  }
+}
+
+template <class T>
+cudaError_t launch_geometric_accumulate(T* acc, size_t n, const T* scalars, const T* points, size_t m, cudaStream_t s) {
+  if (m == 0 || n == 0) return cudaSuccess;
+  const size_t per = (size_t)GA_THREADS * GA_E;
+  geometric_kernel<T><<<(unsigned)((n + per - 1) / per), GA_THREADS, 0, s>>>(acc, n, scalars, points, m);
+  note_launch();
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Geometric accumulation over in-domain points x_j = w_N^(e_j): thread t of a CTA covers
+// i = base + t + u * blockDim (u < E); p = s_j w_N^(e_j i) starts from the root tables and is
+// advanced by w_N^(e_j blockDim) (a base-field multiplier) for each u.
+// ---------------------------------------------------------------------------------------------
+static constexpr int GR_THREADS = 256;
+static constexpr int GR_CHUNK = 256;
+
+template <class T, int E>
+__global__ void __launch_bounds__(GR_THREADS) geometric_roots_kernel(T* acc, uint64_t n, const T* scalars,
+                                                                     const uint64_t* exps, uint64_t m, int logN,
+                                                                     RootTab rt) {
+  typedef typename T::Base B;
+  __shared__ T sS[GR_CHUNK];
+  __shared__ uint64_t sE[GR_CHUNK];
+  __shared__ B sStep[GR_CHUNK];
+  const uint64_t mask = (1ull << logN) - 1;
+  const uint64_t base = (uint64_t)blockIdx.x * GR_THREADS * E;
+  const uint64_t i0 = base + threadIdx.x;
+  T accu[E];
+#pragma unroll
+  for (int u = 0; u < E; ++u) accu[u] = T::zero();
+  for (uint64_t j0 = 0; j0 < m; j0 += GR_CHUNK) {
+    const int cnt = (int)min((uint64_t)GR_CHUNK, m - j0);
+    __syncthreads();
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+      sS[k] = scalars[j0 + k];
+      const uint64_t e = exps[j0 + k] & mask;
+      sE[k] = e;
+      sStep[k] = root_pow<B>(rt, logN, (e * GR_THREADS) & mask);
+    }
+    __syncthreads();
+    for (int j = 0; j < cnt; ++j) {
+      T p = sS[j].mul_base(root_pow<B>(rt, logN, (sE[j] * i0) & mask));
+      const B step = sStep[j];
+#pragma unroll
+      for (int u = 0; u < E; ++u) {
+        accu[u] += p;
+        if (u + 1 < E) p = p.mul_base(step);
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < E; ++u) {
+    const uint64_t i = i0 + (uint64_t)u * GR_THREADS;
+    if (i < n) acc[i] += accu[u];
+  }
+}
+
+template <class T>
+cudaError_t launch_geometric_roots(T* acc, size_t n, const T* scalars, const uint64_t* exps, size_t m, int logN,
+                                   RootTab rt, cudaStream_t s) {
+  if (n == 0 || m == 0) return cudaSuccess;
+  if (logN > rt.log_order) return cudaErrorInvalidValue;
+  int E = 1;
+  while (E < 8 && n / ((size_t)GR_THREADS * E * 2) >= 304) E *= 2;
+  const size_t per = (size_t)GR_THREADS * E;
+  const unsigned grid = (unsigned)((n + per - 1) / per);
+  switch (E) {
+    case 1: geometric_roots_kernel<T, 1><<<grid, GR_THREADS, 0, s>>>(acc, n, scalars, exps, m, logN, rt); break;
+    case 2: geometric_roots_kernel<T, 2><<<grid, GR_THREADS, 0, s>>>(acc, n, scalars, exps, m, logN, rt); break;
+    case 4: geometric_roots_kernel<T, 4><<<grid, GR_THREADS, 0, s>>>(acc, n, scalars, exps, m, logN, rt); break;
+    default: geometric_roots_kernel<T, 8><<<grid, GR_THREADS, 0, s>>>(acc, n, scalars, exps, m, logN, rt); break;
+  }
+  note_launch();
+  return cudaGetLastError();
+}
+
+template <class T>
+__global__ void scatter_kernel(T* dense, const uint64_t* idx, const T* vals, uint64_t m) {
+  for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < m; k += (uint64_t)gridDim.x * blockDim.x)
+    dense[idx[k]] = vals[k];
+}
+template <class T>
+cudaError_t launch_scatter(T* dense, const uint64_t* idx, const T* vals, size_t m, cudaStream_t s) {
+  if (!m) return cudaSuccess;
+  scatter_kernel<T><<<(unsigned)((m + 255) / 256), 256, 0, s>>>(dense, idx, vals, m);
+  note_launch();
+  return cudaGetLastError();
+}
+
+template <class T>
+__global__ void add_kernel(T* acc, const T* src, uint64_t n) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    acc[i] += src[i];
+}
+template <class T>
+cudaError_t launch_add(T* acc, const T* src, size_t n, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  size_t g = std::min<size_t>(SC_MAX_BLOCKS * 2, (n + SC_THREADS - 1) / SC_THREADS);
+  add_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(acc, src, n);
+  note_launch();
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_eq_table(const T* point, int off, int cnt, T scalar, T* table, cudaStream_t s) {
+  eq_table_kernel<T><<<(unsigned)std::max<size_t>(1, ((1ull << cnt) + 255) / 256), 256, 0, s>>>(point, off, cnt,
+                                                                                               scalar, table);
+  note_launch();
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Fused first sumcheck rounds: a = map(x) and b = sum_l rlc_l eq(point_l, .) are evaluated on the
+// fly from the coefficient vector and small eq tables instead of being written to HBM.
+// ---------------------------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ T eq_on_the_fly(const T* tables, int nforms, int h, int l, uint64_t i) {
+  const uint64_t hs = 1ull << h, ls = 1ull << l;
+  T v = T::zero();
+  for (int f = 0; f < nforms; ++f) {
+    const T* hi = tables + (uint64_t)f * (hs + ls);
+    v += hi[i >> l] * hi[hs + (i & (ls - 1))];
+  }
+  return v;
+}
+
+template <class T, class S>
+__global__ void __launch_bounds__(SC_THREADS) first_compute_eq_kernel(const S* x, uint64_t n, const T* tables,
+                                                                      int nforms, int h, int l, T* partials,
+                                                                      T* out, unsigned int* counter) {
+  T acc0 = T::zero(), acc2 = T::zero();
+  const uint64_t half = n >> 1;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < half; i += (uint64_t)gridDim.x * blockDim.x) {
+    const S x0 = x[i], x1 = x[i + half];
+    const T b0 = eq_on_the_fly(tables, nforms, h, l, i), b1 = eq_on_the_fly(tables, nforms, h, l, i + half);
+    acc0 += Embed<T, S>::mul(b0, x0);
+    acc2 += Embed<T, S>::mul(b1 - b0, x1 - x0);
+  }
+  acc0 = block_sum(acc0);
+  acc2 = block_sum(acc2);
+  finish_pairs(acc0, acc2, partials, out, counter);
+}
+
+template <class T, class S>
+__global__ void __launch_bounds__(SC_THREADS) first_fold_compute_eq_kernel(const S* x, uint64_t n, T r,
+                                                                           const T* tables, int nforms, int h, int l,
+                                                                           T* a_out, T* b_out, T* partials, T* out,
+                                                                           unsigned int* counter) {
+  T acc0 = T::zero(), acc2 = T::zero();
+  const uint64_t q = n >> 2, hf = n >> 1;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < q; i += (uint64_t)gridDim.x * blockDim.x) {
+    const S x0 = x[i], x1 = x[i + q], x2 = x[i + hf], x3 = x[i + hf + q];
+    const T fa0 = Embed<T, S>::map(x0) + Embed<T, S>::mul(r, x2 - x0);
+    const T fa1 = Embed<T, S>::map(x1) + Embed<T, S>::mul(r, x3 - x1);
+    const T b0 = eq_on_the_fly(tables, nforms, h, l, i), b1 = eq_on_the_fly(tables, nforms, h, l, i + q);
+    const T b2 = eq_on_the_fly(tables, nforms, h, l, i + hf), b3 = eq_on_the_fly(tables, nforms, h, l, i + hf + q);
+    const T fb0 = b0 + (b2 - b0) * r, fb1 = b1 + (b3 - b1) * r;
+    a_out[i] = fa0;
+    a_out[i + q] = fa1;
+    b_out[i] = fb0;
+    b_out[i + q] = fb1;
+    acc0 += fa0 * fb0;
+    acc2 += (fa1 - fa0) * (fb1 - fb0);
+  }
+  acc0 = block_sum(acc0);
+  acc2 = block_sum(acc2);
+  finish_pairs(acc0, acc2, partials, out, counter);
+}
+
+template <class T, class S>
+cudaError_t launch_first_compute_eq(const S* x, size_t n, const T* tables, int nforms, int nv, T* partials,
+                                    size_t* nparts, cudaStream_t s, T* out, unsigned int* counter) {
+  size_t g = sumcheck_partials(n);
+  first_compute_eq_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(x, n, tables, nforms, nv / 2, nv - nv / 2,
+                                                                    partials, out, counter);
+  note_launch();
+  *nparts = g;
+  return cudaGetLastError();
+}
+template <class T, class S>
+cudaError_t launch_first_fold_compute_eq(const S* x, size_t n, T r, const T* tables, int nforms, int nv, T* a_out,
+                                         T* b_out, T* partials, size_t* nparts, cudaStream_t s, T* out,
+                                         unsigned int* counter) {
+  size_t g = sumcheck_partials(n);
+  first_fold_compute_eq_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(x, n, r, tables, nforms, nv / 2,
+                                                                         nv - nv / 2, a_out, b_out, partials, out,
+                                                                         counter);
+  note_launch();
+  *nparts = g;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Multilinear evaluation sum_i map(x_i) * eq(point, i) with the eq weights taken from one pair of
+// hi / lo tables (tables[0..2^h) and tables[2^h .. 2^h + 2^l)); block sums go to partials.
+// ---------------------------------------------------------------------------------------------
+template <class T, class S>
+__global__ void __launch_bounds__(SC_THREADS) mle_dot_kernel(const S* x, uint64_t n, const T* tables, int h, int l,
+                                                             T* partials) {
+  T acc = T::zero();
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    acc += Embed<T, S>::mul(eq_on_the_fly(tables, 1, h, l, i), x[i]);
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+}
+
+template <class T, class S>
+cudaError_t launch_mle_dot(const S* x, size_t n, const T* tables, int nv, T* partials, size_t* nparts,
+                           cudaStream_t s) {
+  size_t g = std::max<size_t>(1, std::min(SC_MAX_BLOCKS, (n + SC_THREADS - 1) / SC_THREADS));
+  mle_dot_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(x, n, tables, nv / 2, nv - nv / 2, partials);
+  note_launch();
+  *nparts = g;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Lift + RLC
+// ---------------------------------------------------------------------------------------------
+template <class T, class S>
+__global__ void lift_kernel(T* dst, const S* src, uint64_t n) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    dst[i] = Embed<T, S>::map(src[i]);
+}
+template <class T, class S>
+__global__ void axpy_kernel(T* dst, T c, const S* src, uint64_t n) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    dst[i] += Embed<T, S>::mul(c, src[i]);
+}
+
+template <class T, class S>
+cudaError_t launch_lift_rlc(T* dst, const S* const* vecs, const T* coeffs, size_t nvec, size_t n, cudaStream_t s) {
+  size_t g = std::min<size_t>(SC_MAX_BLOCKS * 2, (n + SC_THREADS - 1) / SC_THREADS);
+  if (g == 0) return cudaSuccess;
+  lift_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(dst, vecs[0], n);
+  note_launch();
+  for (size_t j = 1; j < nvec; ++j) {
+    axpy_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(dst, coeffs[j], vecs[j], n);
+    note_launch();
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Univariate evaluation: thread handles UE_E consecutive coefficients by Horner, scaled by
+// x^(chunk start); block sums go to partials.
+// ---------------------------------------------------------------------------------------------
+static constexpr int UE_E = 32;
+
+template <class T, class S>
+__global__ void __launch_bounds__(SC_THREADS) univariate_kernel(const S* c, uint64_t n, T x, T* partials) {
+  const uint64_t start = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * UE_E;
+  T h = T::zero();
+  if (start < n) {
+    const uint64_t end = std::min<uint64_t>(start + UE_E, n);
+    for (uint64_t i = end; i-- > start;) h = h * x + Embed<T, S>::map(c[i]);
+    h = h * x.pow(start);
+  }
+  h = block_sum(h);
+  if (threadIdx.x == 0) partials[blockIdx.x] = h;
+}
+
+template <class T, class S>
+cudaError_t launch_univariate_eval(const S* coeffs, size_t n, T x, T* partials, size_t* nparts, cudaStream_t s) {
+  size_t per = (size_t)SC_THREADS * UE_E;
+  size_t g = std::max<size_t>(1, (n + per - 1) / per);
+  univariate_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(coeffs, n, x, partials);
+  note_launch();
+  *nparts = g;
+  return cudaGetLastError();
+}
+
+// Explicit-instantiation lists (used by sumcheck.cu and sumcheck_mont.cu).
+#define WHIR_SC_INST(T)                                                                                          \
+  template cudaError_t launch_sumcheck_compute<T>(const T*, const T*, size_t, T*, size_t*, cudaStream_t, T*,      \
+                                                  unsigned int*);                                                \
+  template cudaError_t launch_fold_compute<T>(T*, T*, size_t, T, T*, size_t*, cudaStream_t, T*, unsigned int*);  \
+  template cudaError_t launch_fold<T>(T*, size_t, T, cudaStream_t);                                               \
+  template cudaError_t launch_reduce_pairs<T>(const T*, size_t, T*, cudaStream_t);                                \
+  template cudaError_t launch_reduce_singles<T>(const T*, size_t, T*, cudaStream_t);                              \
+  template cudaError_t launch_eval_eq<T>(T*, const T*, int, T, T*, cudaStream_t);                                 \
+  template cudaError_t launch_geometric_accumulate<T>(T*, size_t, const T*, const T*, size_t, cudaStream_t);      \
+  template cudaError_t launch_geometric_roots<T>(T*, size_t, const T*, const uint64_t*, size_t, int, RootTab,    \
+                                                 cudaStream_t);                                                  \
+  template cudaError_t launch_scatter<T>(T*, const uint64_t*, const T*, size_t, cudaStream_t);                   \
+  template cudaError_t launch_add<T>(T*, const T*, size_t, cudaStream_t);                                        \
+  template cudaError_t launch_eq_table<T>(const T*, int, int, T, T*, cudaStream_t);
+
+// Kernels that read coefficient vectors over S and compute over T.
+#define WHIR_SC_EMBED_INST(T, S)                                                                                 \
+  template cudaError_t launch_first_compute_eq<T, S>(const S*, size_t, const T*, int, int, T*, size_t*,          \
+                                                     cudaStream_t, T*, unsigned int*);                           \
+  template cudaError_t launch_first_fold_compute_eq<T, S>(const S*, size_t, T, const T*, int, int, T*, T*, T*,   \
+                                                          size_t*, cudaStream_t, T*, unsigned int*);             \
+  template cudaError_t launch_mle_dot<T, S>(const S*, size_t, const T*, int, T*, size_t*, cudaStream_t);         \
+  template cudaError_t launch_lift_rlc<T, S>(T*, const S* const*, const T*, size_t, size_t, cudaStream_t);       \
+  template cudaError_t launch_univariate_eval<T, S>(const S*, size_t, T, T*, size_t*, cudaStream_t);
+
+}  // namespace whir
