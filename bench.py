@@ -54,6 +54,8 @@ def parse_args():
     ap.add_argument("--batch-jobs", type=int, default=64)
     ap.add_argument("--serve-jobs", type=int, default=48)
     ap.add_argument("--workers", type=int, default=4)
+    ap.add_argument("--multilimb-nv", type=int, default=20)
+    ap.add_argument("--no-multilimb", action="store_true", help="skip the Field256 / Field192 measurement")
     return ap.parse_args()
 
 
@@ -205,6 +207,76 @@ def batched_and_serving(args, dev):
         "p99_ms": float(np.percentile(lat, 99)) * 1e3, "proofs_per_s": len(sjobs) / wall, "workers": args.workers,
         "bit_exact_vs_plain": all((j.narg, j.hints) == r for j, r in zip(sjobs, sref)),
         "timing": "host wall clock"}
+    return out
+
+
+def multilimb(args, dev):
+    """Multi-limb workload: WHIR PCS commit+prove at d=20 over Field256 then Field192 (Montgomery form),
+    SHA3 Merkle trees, rate 1/4, k=4, security 128 list decoding, pow 20, 4 uniform random evaluation
+    points. Device-resident input, CUDA events on the context's stream; proof bytes checked identical
+    across steps. The CPU column times the oracle prover on the same input (one proof per field)."""
+    import torch
+
+    import whir_gb300 as W
+    from whir_gb300.inputs import Rng, field_elements
+    nv = args.multilimb_nv
+    ctx = W.Context(dev)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=dev)
+    params = W.ProtocolParameters(unique_decoding=False, security_level=128, pow_bits=20, starting_log_inv_rate=2,
+                                  initial_folding_factor=4, folding_factor=4, hash_id="Sha3")
+    out = {"workload": "WHIR PCS commit+prove d=%d, SHA3, rate 1/4, k=4, sec 128 list decoding, pow 20, 4 points"
+                       % nv}
+    for field in ("Field256", "Field192"):
+        fid = W.FIELDS[field]
+        r = Rng(fid * 20)
+        vec = field_elements(field, 1 << nv, rng=r).reshape(-1)
+        pts = [field_elements(field, nv, rng=r).reshape(-1) for _ in range(4)]
+        evs = [[W.multilinear_evaluate(ctx, fid, vec, p)] for p in pts]
+        cfg = W.Config(field, 1 << nv, params)
+        d_vec = ctx.alloc(vec.nbytes)
+        ctx.upload(d_vec, vec)
+
+        def one():
+            ps = W.ProverState(cfg, "bench " + field)
+            w = cfg.commit(ctx, ps, d_vec, on_device=True)
+            cfg.prove(ctx, ps, d_vec, [w], pts, [], evs, on_device=True)
+            w.free()
+            return ps.proof()
+
+        ref = None
+        for _ in range(2):
+            ref = one()
+        ctx.set_profiling(True)
+        times = []
+        for _ in range(max(3, args.steps // 2)):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            got = one()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            assert got == ref, "proof bytes changed between runs"
+        prof = ctx.profile()
+        ctx.set_profiling(False)
+        ctx.free(d_vec)
+        entry = {"prove_ms": float(np.mean(times)), "p50_ms": float(np.percentile(times, 50)),
+                 "kernel_families_ms_per_proof": {k: v[0] / len(times) for k, v in prof.items() if v[1]},
+                 "narg_bytes": len(ref[0]), "hint_bytes": len(ref[1])}
+        if not args.no_cpu_baseline:
+            import oracle
+            op = oracle.make_params(unique_decoding=False, security_level=128, pow_bits=20, starting_log_inv_rate=2,
+                                    hash_id=oracle.ENGINE_SHA3)
+            vv = vec.reshape(1, 1 << nv, -1)
+            pp = [p.reshape(nv, -1) for p in pts]
+            t0 = time.perf_counter()
+            pr = oracle.whir_prove(fid, op, nv, "bench " + field, vv, pp, [], evs)
+            sec = time.perf_counter() - t0
+            entry["cpu_baseline"] = {"value": sec * 1e3, "unit": "ms", "cores": oracle.lib().oracle_num_threads(),
+                                     "kind": "port", "sample": "1 proof, same input"}
+            entry["bit_exact_vs_cpu"] = (pr.narg, pr.hints) == ref
+        out[field] = entry
+    ctx.close()
     return out
 
 
@@ -402,6 +474,8 @@ def run_gpu(args):
                     "frac": None, "traffic": None, "avg_launch_ms": ms_f / calls_f}
     cpu = None if args.no_cpu_baseline else cpu_baseline(args, params, vec, point)
     extra = {} if args.no_batch else batched_and_serving(args, dev)
+    if not args.no_multilimb:
+        extra["multilimb"] = multilimb(args, dev)
     line = {
         "metric": "prove_ms_d%d_goldilocks2_blake3" % nv, "value": ms_per_proof_job, "unit": "ms",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(times)),
