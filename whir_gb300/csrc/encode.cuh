@@ -25,17 +25,73 @@ namespace whir {
 static constexpr int ENC_THREADS = 256;
 static constexpr size_t ENC_SMEM_BUDGET = 64 * 1024;  // data bytes per CTA
 static constexpr int ENC_MAX_LOGN_SMEM = 12;          // largest in-CTA NTT
-// Dynamic shared memory limit set on the encode kernels: the data tile plus up to half its size in
-// twiddles (n/2 base elements for a size-n NTT) plus alignment slack.
-static constexpr size_t ENC_SMEM_ATTR = ENC_SMEM_BUDGET + ENC_SMEM_BUDGET / 2 + 256;
+// Dynamic shared memory limit set on the encode kernels: the data tile plus at most as many bytes
+// of twiddles (n - 1 base elements for a size-n NTT) plus alignment slack.
+static constexpr size_t ENC_SMEM_ATTR = 2 * ENC_SMEM_BUDGET + 256;
 
+
+// Shared-memory element index swizzle: the low SB bits of an element index are XORed with the XOR
+// of its higher SB-bit groups (a bijection within each aligned block of 2^SB elements). The NTT
+// steps' power-of-two strides, the bit-reversed row order of the row stores and of the leaf hashing,
+// and the interleaved columns of the four-step pass then spread over the 32 banks instead of
+// landing on one or two.
+template <class F>
+struct SwzBits {
+  static constexpr int value = sizeof(F) == 16 ? 3 : (sizeof(F) == 32 ? 2 : 4);
+};
+template <class F>
+__device__ __forceinline__ int swz(int L) {
+  constexpr int SB = SwzBits<F>::value;
+  int h = 0;
+#pragma unroll
+  for (int sh = SB; sh < 15; sh += SB) h ^= L >> sh;
+  return L ^ (h & ((1 << SB) - 1));
+}
+// Shared-memory element access, 16-byte vectorised where the element size allows it.
+template <class F>
+__device__ __forceinline__ F lds(const F* s, int i) {
+  if constexpr (sizeof(F) % 16 == 0) {
+    F r;
+    const ulonglong2* p = reinterpret_cast<const ulonglong2*>(s + i);
+    ulonglong2* d = reinterpret_cast<ulonglong2*>(&r);
+#pragma unroll
+    for (int q = 0; q < (int)(sizeof(F) / 16); ++q) d[q] = p[q];
+    return r;
+  } else {
+    return s[i];
+  }
+}
+template <class F>
+__device__ __forceinline__ void sts(F* s, int i, const F& x) {
+  if constexpr (sizeof(F) % 16 == 0) {
+    ulonglong2* p = reinterpret_cast<ulonglong2*>(s + i);
+    const ulonglong2* d = reinterpret_cast<const ulonglong2*>(&x);
+#pragma unroll
+    for (int q = 0; q < (int)(sizeof(F) / 16); ++q) p[q] = d[q];
+  } else {
+    s[i] = x;
+  }
+}
+
+// NTT twiddles by butterfly span: level L (span 2h = 2^L) holds w_(2h)^q for q < h at offset h - 1,
+// so the threads of a warp read consecutive entries. The table is in shared memory, or (TWG) read
+// through L1 from the global copy.
+template <class B, bool TWG>
+__device__ __forceinline__ B level_tw(const B* tw, int log2h, int pos) {
+  const int i = (1 << (log2h - 1)) - 1 + pos;
+  if constexpr (TWG) {
+    return ldg_elem(tw + i);
+  } else {
+    return tw[i];
+  }
+}
 
 // LOGR consecutive decimation-in-frequency stages done in registers. The current sub-blocks have
 // size B = 2^logB; a work item (vector v, sub-block blk, offset j < B/R) owns the R = 2^LOGR
 // elements at offsets j + k*B/R, k < R, which are exactly the elements those stages combine.
 // Stage st pairs k with k + R/2^(st+1) and multiplies the difference by w_(2h)^(offset mod 2h),
-// 2h = B / 2^st, read from tw[q] = w_n^q.
-template <class F, int LOGR>
+// 2h = B / 2^st.
+template <class F, int LOGR, bool TWG>
 __device__ __forceinline__ void dif_step(F* s, int logn, int logB, int nvec, int lognvec, int vs, int es,
                                          bool vec_fastest, const typename F::Base* tw) {
   constexpr int R = 1 << LOGR;
@@ -53,45 +109,55 @@ __device__ __forceinline__ void dif_step(F* s, int logn, int logB, int nvec, int
       it = t & ((1 << items_log) - 1);
     }
     const int blk = it >> logstride, j = it & (stride - 1);
-    F* base = s + v * vs + (((blk << logB) + j) * es);
+    const int base = v * vs + (((blk << logB) + j) * es);
     const int kstep = stride * es;
+    int pidx[R];
     F x[R];
 #pragma unroll
-    for (int k = 0; k < R; ++k) x[k] = base[k * kstep];
+    for (int k = 0; k < R; ++k) {
+      pidx[k] = swz<F>(base + k * kstep);
+      x[k] = lds(s, pidx[k]);
+    }
 #pragma unroll
     for (int st = 0; st < LOGR; ++st) {
       const int half = R >> (st + 1);
       const int log2h = logB - st;
-      const int tws = logn - log2h;
 #pragma unroll
       for (int k = 0; k < R; ++k) {
         if (k & half) continue;
         const int pos = (j + k * stride) & ((1 << log2h) - 1);
         const F u = x[k], w = x[k + half];
         x[k] = u + w;
-        x[k + half] = (u - w).mul_base(tw[pos << tws]);
+        x[k + half] = (u - w).mul_base(level_tw<typename F::Base, TWG>(tw, log2h, pos));
       }
     }
 #pragma unroll
-    for (int k = 0; k < R; ++k) base[k * kstep] = x[k];
+    for (int k = 0; k < R; ++k) sts(s, pidx[k], x[k]);
   }
   __syncthreads();
 }
 
 // In-place DIF NTT of nvec vectors of size 2^logn in shared memory; element i of vector v lives at
-// s[v*vs + i*es]. Output index k ends up at position brev(k). Stages are processed three at a time
-// in registers (radix 8), with a radix-4 / radix-2 step for the remainder.
-template <class F>
+// s[swz(v*vs + i*es)]. Output index k ends up at position brev(k). Stages are processed three at a
+// time in registers (radix 8), with a radix-4 / radix-2 step for the remainder.
+template <class F, bool TWG>
 __device__ void smem_ntt_dif(F* s, int logn, int nvec, int vs, int es, bool vec_fastest, const typename F::Base* tw) {
   int lognvec = 0;
   while ((1 << lognvec) < nvec) ++lognvec;
   int logB = logn;
   while (logB >= 3) {
-    dif_step<F, 3>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
+    dif_step<F, 3, TWG>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
     logB -= 3;
   }
-  if (logB == 2) dif_step<F, 2>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
-  if (logB == 1) dif_step<F, 1>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
+  if (logB == 2) dif_step<F, 2, TWG>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
+  if (logB == 1) dif_step<F, 1, TWG>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
+}
+
+// Copies the twiddle levels 1..logn (entries [0, 2^logn - 1)) of the global table into shared memory.
+template <class B>
+__device__ __forceinline__ void load_twiddles(B* tw, const RootTab& rt, int logn) {
+  const B* g = reinterpret_cast<const B*>(rt.ntt);
+  for (int k = threadIdx.x; k < (1 << logn) - 1; k += blockDim.x) tw[k] = ldg_elem(g + k);
 }
 
 // 32-bit little-endian words of an element's u64 limbs (the element must already be canonical).
@@ -133,32 +199,35 @@ __global__ void __launch_bounds__(ENC_THREADS) encode_rows_kernel(EncArgs<F> a) 
   typedef typename F::Base B;
   B* tw = reinterpret_cast<B*>(smem_raw + (size_t)nvec * n * sizeof(F));
   const uint64_t C = 1ull << a.logC, N = 1ull << a.logN;
-  for (int k = threadIdx.x; k < (n >> 1); k += blockDim.x) tw[k] = root_pow<B>(a.rt, logn, (uint64_t)k);
+  load_twiddles<B>(tw, a.rt, logn);
 
   uint64_t c_base = 0, k1 = 0;
   if (a.mode == 0) {
     c_base = (uint64_t)blockIdx.x * a.G;
+    #pragma unroll 4
     for (int idx = threadIdx.x; idx < nvec * n; idx += blockDim.x) {
       const int vec = idx >> logn, j = idx & (n - 1);
       const int g = vec / M, m = vec - g * M;
       const uint64_t c = c_base + g;
       F x = (uint64_t)j < a.msg_len ? a.src[(uint64_t)m * a.msg_len + j] : F::zero();
       if (c != 0 && j != 0) x = x.mul_base(root_pow<B>(a.rt, a.logN, (c * (uint64_t)j) & (N - 1)));
-      s[idx] = x;
+      sts(s, swz<F>(idx), x);
     }
   } else {
     const uint64_t C1 = 1ull << a.logC1;
     c_base = blockIdx.x >> a.logC1;
     k1 = blockIdx.x & (C1 - 1);
+    #pragma unroll 4
     for (int idx = threadIdx.x; idx < M * n; idx += blockDim.x) {
       const int m = idx >> logn, j2 = idx & (n - 1);
-      s[idx] = a.src[((((uint64_t)m * a.K + c_base) << a.logC1) + k1) * n + j2];
+      sts(s, swz<F>(idx), a.src[((((uint64_t)m * a.K + c_base) << a.logC1) + k1) * n + j2]);
     }
   }
   __syncthreads();
-  smem_ntt_dif<F>(s, logn, nvec, n, 1, false, tw);
+  smem_ntt_dif<F, false>(s, logn, nvec, n, 1, false, tw);
 
   // Coalesced row stores: consecutive threads write consecutive columns of consecutive rows.
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < R * M; idx += blockDim.x) {
     const int rho = idx / M, m = idx - rho * M;
     uint64_t row;
@@ -171,7 +240,7 @@ __global__ void __launch_bounds__(ENC_THREADS) encode_rows_kernel(EncArgs<F> a) 
       row = c_base * C + k1 + ((uint64_t)rho << a.logC1);
       sidx = (m << logn) + brev(rho, logn);
     }
-    a.dst[row * M + m] = s[sidx];
+    a.dst[row * M + m] = lds(s, swz<F>(sidx));
   }
   if (a.leaves == nullptr) return;
   if constexpr (!Canon<F>::IDENTITY) {
@@ -214,7 +283,7 @@ __global__ void __launch_bounds__(ENC_THREADS) encode_rows_kernel(EncArgs<F> a) 
           uint64_t limb = 0;
           if (L < limbs) {
             const int col = L / F::LIMBS, part = L - col * F::LIMBS;
-            limb = reinterpret_cast<const uint64_t*>(&s[base + (col << logn)])[part];
+            limb = reinterpret_cast<const uint64_t*>(&s[swz<F>(base + (col << logn))])[part];
           }
           mw[2 * q] = (uint32_t)limb;
           mw[2 * q + 1] = (uint32_t)(limb >> 32);
@@ -229,7 +298,7 @@ __global__ void __launch_bounds__(ENC_THREADS) encode_rows_kernel(EncArgs<F> a) 
       h.init((uint32_t)(M * F::LIMBS * 8));
       for (int m = 0; m < M; ++m) {
         uint32_t w[2 * F::LIMBS];
-        push_elem_words<F>(s[base + (m << logn)], w);
+        push_elem_words<F>(lds(s, swz<F>(base + (m << logn))), w);
 #pragma unroll
         for (int q = 0; q < 2 * F::LIMBS; ++q) h.push(w[q]);
       }
@@ -249,29 +318,63 @@ __global__ void __launch_bounds__(ENC_THREADS) encode_cols_kernel(EncArgs<F> a) 
   F* s = reinterpret_cast<F*>(smem_raw);
   const int logn = a.logC1, n = 1 << logn, W = a.W;
   typedef typename F::Base B;
-  B* tw = reinterpret_cast<B*>(smem_raw + (size_t)W * n * sizeof(F));
+  const B* tw = reinterpret_cast<const B*>(a.rt.ntt);  // read through L1 (keeps shared memory for data)
   const uint64_t C2 = 1ull << a.logC2, N = 1ull << a.logN;
   const uint64_t tiles = C2 / W;
   const uint64_t tile = blockIdx.x % tiles;
   const uint64_t mc = blockIdx.x / tiles;  // m * K + c
   const uint64_t c = mc % a.K, m = mc / a.K;
-  for (int k = threadIdx.x; k < (n >> 1); k += blockDim.x) tw[k] = root_pow<B>(a.rt, logn, (uint64_t)k);
-  for (int idx = threadIdx.x; idx < n * W; idx += blockDim.x) {
-    const int j1 = idx / W, w = idx - j1 * W;
-    const uint64_t j = ((uint64_t)j1 << a.logC2) + tile * W + w;
-    F x = j < a.msg_len ? a.src[m * a.msg_len + j] : F::zero();
-    if (c != 0 && j != 0) x = x.mul_base(root_pow<B>(a.rt, a.logN, (c * j) & (N - 1)));
-    s[idx] = x;
+  // With W dividing the block size every thread keeps one column w, and its successive elements
+  // are js = ENC_THREADS / W rows apart: the coset twist w_N^(c j) and the four-step twiddle
+  // w_C^(j2 k1) then advance by a constant factor per element instead of two table reads each.
+  const bool fixed_col = ENC_THREADS % W == 0;
+  const int js = ENC_THREADS / W;
+  if (fixed_col) {
+    const int w = threadIdx.x % W;
+    const uint64_t j2 = tile * W + w;
+    B t = root_pow<B>(a.rt, a.logN, (c * ((((uint64_t)threadIdx.x / W) << a.logC2) + j2)) & (N - 1));
+    const B step = root_pow<B>(a.rt, a.logN, (c * ((uint64_t)js << a.logC2)) & (N - 1));
+    for (int idx = threadIdx.x; idx < n * W; idx += blockDim.x) {
+      const uint64_t j = ((uint64_t)(idx / W) << a.logC2) + j2;
+      F x = j < a.msg_len ? a.src[m * a.msg_len + j] : F::zero();
+      if (c != 0) {
+        x = x.mul_base(t);
+        t = t * step;
+      }
+      sts(s, swz<F>(idx), x);
+    }
+  } else {
+    for (int idx = threadIdx.x; idx < n * W; idx += blockDim.x) {
+      const int j1 = idx / W, w = idx - j1 * W;
+      const uint64_t j = ((uint64_t)j1 << a.logC2) + tile * W + w;
+      F x = j < a.msg_len ? a.src[m * a.msg_len + j] : F::zero();
+      if (c != 0 && j != 0) x = x.mul_base(root_pow<B>(a.rt, a.logN, (c * j) & (N - 1)));
+      sts(s, swz<F>(idx), x);
+    }
   }
   __syncthreads();
-  smem_ntt_dif<F>(s, logn, W, 1, W, true, tw);
-  for (int idx = threadIdx.x; idx < n * W; idx += blockDim.x) {
-    const int k1 = idx / W, w = idx - k1 * W;
+  smem_ntt_dif<F, true>(s, logn, W, 1, W, true, tw);
+  const uint64_t cmask = (1ull << a.logC) - 1;
+  if (fixed_col) {
+    const int w = threadIdx.x % W;
     const uint64_t j2 = tile * W + w;
-    F v = s[brev(k1, logn) * W + w];
-    const uint64_t e = j2 * (uint64_t)k1;
-    if (e) v = v.mul_base(root_pow<B>(a.rt, a.logC, e));
-    a.dst[((mc << a.logC1) + k1) * C2 + j2] = v;
+    B t = root_pow<B>(a.rt, a.logC, (j2 * (uint64_t)(threadIdx.x / W)) & cmask);
+    const B step = root_pow<B>(a.rt, a.logC, (j2 * (uint64_t)js) & cmask);
+    for (int idx = threadIdx.x; idx < n * W; idx += blockDim.x) {
+      const int k1 = idx / W;
+      F v = lds(s, swz<F>(brev(k1, logn) * W + w)).mul_base(t);
+      t = t * step;
+      a.dst[((mc << a.logC1) + k1) * C2 + j2] = v;
+    }
+  } else {
+    for (int idx = threadIdx.x; idx < n * W; idx += blockDim.x) {
+      const int k1 = idx / W, w = idx - k1 * W;
+      const uint64_t j2 = tile * W + w;
+      F v = lds(s, swz<F>(brev(k1, logn) * W + w));
+      const uint64_t e = j2 * (uint64_t)k1;
+      if (e) v = v.mul_base(root_pow<B>(a.rt, a.logC, e));
+      a.dst[((mc << a.logC1) + k1) * C2 + j2] = v;
+    }
   }
 }
 
@@ -319,7 +422,7 @@ cudaError_t launch_encode(const EncodePlan& p, const F* src, size_t n_msgs, size
     a.src = src;
     a.dst = dst;
     const size_t n = 1ull << p.logC;
-    const size_t smem = (size_t)a.G * n_msgs * n * sizeof(F) + (n / 2) * sizeof(typename F::Base) + 16;
+    const size_t smem = (size_t)a.G * n_msgs * n * sizeof(F) + n * sizeof(typename F::Base) + 16;
     return dispatch_rows<F>(a, hash_kind, (unsigned)(a.K / a.G), smem, s);
   }
   // pass 1
@@ -332,7 +435,7 @@ cudaError_t launch_encode(const EncodePlan& p, const F* src, size_t n_msgs, size
     c.dst = scratch;
     c.leaves = nullptr;
     const size_t C1 = 1ull << p.logC1, C2 = 1ull << p.logC2;
-    const size_t smem = (size_t)a.W * C1 * sizeof(F) + (C1 / 2) * sizeof(typename F::Base) + 16;
+    const size_t smem = (size_t)a.W * C1 * sizeof(F) + 16;
     const size_t grid = n_msgs * a.K * (C2 / a.W);
     encode_cols_kernel<F><<<(unsigned)grid, ENC_THREADS, smem, s>>>(c);
     note_launch();
@@ -344,7 +447,7 @@ cudaError_t launch_encode(const EncodePlan& p, const F* src, size_t n_msgs, size
   a.src = scratch;
   a.dst = dst;
   const size_t C1 = 1ull << p.logC1, C2 = 1ull << p.logC2;
-  const size_t smem = n_msgs * C2 * sizeof(F) + (C2 / 2) * sizeof(typename F::Base) + 16;
+  const size_t smem = n_msgs * C2 * sizeof(F) + C2 * sizeof(typename F::Base) + 16;
   return dispatch_rows<F>(a, hash_kind, (unsigned)(a.K * C1), smem, s);
 }
 

@@ -17,10 +17,13 @@ void note_launch();
 
 // Powers of the 2^log_order-th root of unity w of a base prime field, stored as base-field elements
 // (Montgomery form for Field192/Field256): lo[i] = w^i (i < 2^16), hi[i] = w^(i * 2^16)
-// (i < 2^(log_order - 16)).
+// (i < 2^(log_order - 16)). ntt: the in-CTA NTT twiddles by level, level L = 1..NTT_TW_LEVELS
+// holding w_(2^L)^q for q < 2^(L-1) at offset 2^(L-1) - 1.
+static constexpr int NTT_TW_LEVELS = 12;
 struct RootTab {
   const uint64_t* lo;
   const uint64_t* hi;
+  const uint64_t* ntt;
   int log_order;
 };
 

@@ -7,7 +7,7 @@
 // expressions; the host compiler runs with -ffp-contract=off so no fused multiply-add changes a
 // rounding. The transcript has the reference's interaction structure (src/transcript/mod.rs) on a
 // Keccak-f[1600] duplex sponge of this library (the reference's spongefish sponge is not
-// available); its exact byte rules are documented on DuplexSponge below.
+// available); its exact byte rules are documented in sponge.cuh.
 #pragma once
 #include <algorithm>
 #include <cmath>
@@ -18,6 +18,7 @@
 
 #include "field.cuh"
 #include "hash.cuh"
+#include "sponge.cuh"
 
 namespace whir {
 
@@ -106,61 +107,15 @@ inline void host_hash(int kind, const uint8_t* msg, size_t len, uint8_t out[32])
 }
 
 // ---------------------------------------------------------------------------------------------
-// Transcript
+// Transcript (the sponge and its byte rules are in sponge.cuh)
 // ---------------------------------------------------------------------------------------------
-// Duplex sponge over Keccak-f[1600], rate 136 bytes:
-//   absorb  — XOR bytes into the rate, permuting before a byte that would overflow it;
-//   squeeze — on the first squeeze after absorbing, XOR 0x01 at the current position and 0x80 at
-//             rate byte 135, permute, then read rate bytes (permuting when exhausted).
-// Initialised by absorbing protocol_id (64 bytes) then session_id (32 bytes).
-struct DuplexSponge {
-  uint64_t st[25];
-  size_t pos = 0;
-  bool squeezing = false;
-  static constexpr size_t RATE = 136;
-  DuplexSponge() { memset(st, 0, sizeof(st)); }
-  uint8_t* bytes() { return reinterpret_cast<uint8_t*>(st); }
-  void absorb(const uint8_t* in, size_t n) {
-    if (squeezing) {
-      squeezing = false;
-      pos = 0;
-    }
-    for (size_t i = 0; i < n; ++i) {
-      if (pos == RATE) {
-        keccak_f1600(st);
-        pos = 0;
-      }
-      bytes()[pos++] ^= in[i];
-    }
-  }
-  void squeeze(uint8_t* out, size_t n) {
-    if (!squeezing) {
-      if (pos == RATE) {
-        keccak_f1600(st);
-        pos = 0;
-      }
-      bytes()[pos] ^= 0x01;
-      bytes()[RATE - 1] ^= 0x80;
-      keccak_f1600(st);
-      pos = 0;
-      squeezing = true;
-    }
-    for (size_t i = 0; i < n; ++i) {
-      if (pos == RATE) {
-        keccak_f1600(st);
-        pos = 0;
-      }
-      out[i] = bytes()[pos++];
-    }
-  }
-};
-
 // ProverState: NARG string (prover messages, absorbed) plus out-of-band hints (not absorbed).
 struct Transcript {
-  DuplexSponge sponge;
+  Sponge sponge;
   std::vector<uint8_t> narg, hints;
+  Transcript() { sponge.reset(); }
   void init(const uint8_t protocol_id[64], const uint8_t session_id[32]) {
-    sponge = DuplexSponge();
+    sponge.reset();
     narg.clear();
     hints.clear();
     sponge.absorb(protocol_id, 64);
@@ -195,18 +150,8 @@ inline std::vector<uint8_t> cbor_text(const std::string& s) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// Element codecs: ArkFieldEncoder bytes are the canonical little-endian bytes of each base
-// coefficient, 8 per Goldilocks coefficient, 24 for Field192 and 32 for Field256 (exactly the
-// canonical u64 limbs of the element in every supported field).
+// Element codecs on the transcript (byte rules in sponge.cuh)
 // ---------------------------------------------------------------------------------------------
-template <class F>
-inline void elem_bytes(const F& x, uint8_t* out) {
-  static_assert(F::LIMBS * 8 == F::DEG * Canon<F>::BASE_BYTES, "encoded size must equal the limb size");
-  uint64_t c[F::LIMBS];
-  Canon<F>::to(x, c);
-  for (int d = 0; d < F::LIMBS; ++d)
-    for (int i = 0; i < 8; ++i) out[8 * d + i] = (uint8_t)(c[d] >> (8 * i));
-}
 template <class F>
 inline void send_elem(Transcript& t, const F& x) {
   uint8_t b[8 * F::LIMBS];
@@ -225,71 +170,10 @@ inline F get_raw(const uint64_t* w) {
   memcpy(&x, w, sizeof(F));
   return x;
 }
-
-// verifier_message<F>: per base coefficient squeeze (base bytes + 16) bytes, read as a
-// little-endian integer and reduced mod p.
-inline Gl gl_from_bytes_mod(const uint8_t* b, size_t n) {
-  uint64_t acc = 0;
-  const uint64_t two64 = GL_EPS;
-  size_t words = (n + 7) / 8;
-  for (size_t w = words; w-- > 0;) {
-    uint64_t x = 0;
-    for (int i = 7; i >= 0; --i) {
-      size_t k = w * 8 + i;
-      x = (x << 8) | (k < n ? b[k] : 0);
-    }
-    if (x >= GL_P) x -= GL_P;
-    acc = gl_add(gl_mul(acc, two64), x);
-  }
-  return Gl{acc};
-}
-template <class P>
-inline MontField<P> mont_from_bytes_mod(const uint8_t* b, size_t n) {
-  typedef MontField<P> M;
-  uint64_t l[M::N] = {0};
-  l[1] = 1;
-  const M two64 = M::from_canonical(l);
-  M acc = M::zero();
-  size_t words = (n + 7) / 8;
-  for (size_t w = words; w-- > 0;) {
-    uint64_t x = 0;
-    for (int i = 7; i >= 0; --i) {
-      size_t k = w * 8 + i;
-      x = (x << 8) | (k < n ? b[k] : 0);
-    }
-    uint64_t xl[M::N] = {0};
-    xl[0] = x;
-    acc = acc * two64 + M::from_canonical(xl);
-  }
-  return acc;
-}
-
-template <class F>
-struct ChallengeCodec {
-  // Goldilocks family: DEG coefficients of 8 + 16 squeezed bytes each.
-  static F squeeze(Transcript& t) {
-    uint64_t c[F::LIMBS];
-    uint8_t buf[24];
-    for (int d = 0; d < F::DEG; ++d) {
-      t.verifier_bytes(buf, 24);
-      c[d] = gl_from_bytes_mod(buf, 24).v;
-    }
-    return Canon<F>::from(c);
-  }
-};
-template <class P>
-struct ChallengeCodec<MontField<P>> {
-  static MontField<P> squeeze(Transcript& t) {
-    uint8_t buf[P::BYTES + 16];
-    t.verifier_bytes(buf, sizeof(buf));
-    return mont_from_bytes_mod<P>(buf, sizeof(buf));
-  }
-};
 template <class F>
 inline F challenge(Transcript& t) {
-  return ChallengeCodec<F>::squeeze(t);
+  return ChallengeCodec<F>::squeeze(t.sponge);
 }
-
 template <class F>
 inline std::vector<F> geometric_challenge(Transcript& t, size_t count) {
   if (count == 0) return {};

@@ -235,10 +235,10 @@ const RootTab& root_tab(whir_ctx* ctx) {
   constexpr int k = RootSlot<B>::value;
   if (!ctx->d_roots[k]) {
     const int L = RootInfo<B>::TABLE_LOG;
-    const size_t nlo = 1u << 16, nhi = (size_t)1 << (L - 16);
+    const size_t nlo = 1u << 16, nhi = (size_t)1 << (L - 16), nntt = ((size_t)1 << NTT_TW_LEVELS) - 1;
     const B w = RootInfo<B>::root(1ull << L);
     const B w16 = w.pow(1ull << 16);
-    std::vector<B> tab(nlo + nhi);
+    std::vector<B> tab(nlo + nhi + nntt);
     B x = B::one(), y = B::one();
     for (size_t i = 0; i < nlo; ++i) {
       tab[i] = x;
@@ -248,12 +248,22 @@ const RootTab& root_tab(whir_ctx* ctx) {
       tab[nlo + i] = y;
       y = y * w16;
     }
+    for (int lev = 1; lev <= NTT_TW_LEVELS; ++lev) {
+      const size_t h = (size_t)1 << (lev - 1);
+      const B wl = w.pow(1ull << (L - lev));  // root(2^lev)
+      B z = B::one();
+      for (size_t q = 0; q < h; ++q) {
+        tab[nlo + nhi + h - 1 + q] = z;
+        z = z * wl;
+      }
+    }
     uint64_t* d = nullptr;
     CU(cudaMalloc((void**)&d, tab.size() * sizeof(B)));
     CU(cudaMemcpy(d, tab.data(), tab.size() * sizeof(B), cudaMemcpyHostToDevice));
     ctx->d_roots[k] = d;
     ctx->rts[k].lo = d;
     ctx->rts[k].hi = d + nlo * (sizeof(B) / 8);
+    ctx->rts[k].ntt = d + (nlo + nhi) * (sizeof(B) / 8);
     ctx->rts[k].log_order = L;
   }
   return ctx->rts[k];
