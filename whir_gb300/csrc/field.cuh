@@ -94,9 +94,9 @@ __device__ __forceinline__ uint64_t gl_mul_ptx(uint64_t a, uint64_t b) {
       "subc.u32 bw, z, z;\n\t"
       "sub.cc.u32 r0, r0, bw;\n\t"
       "subc.u32 r1, r1, z;\n\t"
-      // y = r2 * (2^32 - 1) = (r2 << 32) - r2
-      "sub.cc.u32 y0, z, r2;\n\t"
-      "subc.u32 y1, r2, z;\n\t"
+      // y = r2 * (2^32 - 1) as one 32x32 -> 64 multiply (integer multiply pipe)
+      "mul.lo.u32 y0, r2, 0xffffffff;\n\t"
+      "mul.hi.u32 y1, r2, 0xffffffff;\n\t"
       // w += y, plus eps on carry
       "add.cc.u32 r0, r0, y0;\n\t"
       "addc.cc.u32 r1, r1, y1;\n\t"
@@ -158,10 +158,15 @@ WHIR_HD uint64_t gl_mul(uint64_t a, uint64_t b) {
 #endif
 }
 WHIR_HD uint64_t gl_sqr(uint64_t a) { return gl_mul(a, a); }
-// 7 * a as 8a - a with modular additions (cheaper than a multiply).
+// 7 * a (the non-residue of Fp2). On the device a multiply: its products run on the integer
+// multiply pipe, which the add/select-heavy field code leaves mostly idle.
 WHIR_HD uint64_t gl_mul7(uint64_t a) {
+#if defined(__CUDA_ARCH__)
+  return gl_mul_ptx(a, 7);
+#else
   uint64_t a2 = gl_add(a, a), a4 = gl_add(a2, a2), a8 = gl_add(a4, a4);
   return gl_sub(a8, a);
+#endif
 }
 WHIR_HD uint64_t gl_pow(uint64_t a, uint64_t e) {
   uint64_t r = 1;
