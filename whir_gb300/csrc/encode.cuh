@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "field.cuh"
 #include "hash.cuh"
@@ -378,11 +379,28 @@ __global__ void __launch_bounds__(ENC_THREADS) encode_cols_kernel(EncArgs<F> a) 
   }
 }
 
+// Raises a kernel's dynamic shared-memory limit once per device. Each caller instantiation owns its
+// flags; std::call_once makes concurrent first launches from several host threads wait for the one
+// that sets the attribute.
+static constexpr int ENC_MAX_DEVICES = 64;
+template <class K>
+static cudaError_t smem_attr_once(K kernel, std::once_flag* flags, cudaError_t* results) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= ENC_MAX_DEVICES)
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ENC_SMEM_ATTR);
+  std::call_once(flags[dev], [&] {
+    results[dev] = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ENC_SMEM_ATTR);
+  });
+  return results[dev];
+}
+
 template <class F, int KIND>
 static cudaError_t run_rows(const EncArgs<F>& a, unsigned grid, size_t smem, cudaStream_t s) {
-  // Set on every launch: the attribute is per device and this may run from several host threads.
-  cudaError_t e = cudaFuncSetAttribute(encode_rows_kernel<F, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)ENC_SMEM_ATTR);
+  static std::once_flag flags[ENC_MAX_DEVICES];
+  static cudaError_t results[ENC_MAX_DEVICES];
+  cudaError_t e = smem_attr_once(encode_rows_kernel<F, KIND>, flags, results);
   if (e != cudaSuccess) return e;
   encode_rows_kernel<F, KIND><<<grid, ENC_THREADS, smem, s>>>(a);
   note_launch();
@@ -427,8 +445,9 @@ cudaError_t launch_encode(const EncodePlan& p, const F* src, size_t n_msgs, size
   }
   // pass 1
   {
-    cudaError_t ea = cudaFuncSetAttribute(encode_cols_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)ENC_SMEM_ATTR);
+    static std::once_flag flags[ENC_MAX_DEVICES];
+    static cudaError_t results[ENC_MAX_DEVICES];
+    cudaError_t ea = smem_attr_once(encode_cols_kernel<F>, flags, results);
     if (ea != cudaSuccess) return ea;
     EncArgs<F> c = a;
     c.src = src;

@@ -28,17 +28,19 @@ static constexpr uint64_t GL_EPS = 0xFFFFFFFFULL;
 // ALU pipe than the 64-bit C expressions). Same canonical inputs and outputs as the host versions.
 __device__ __forceinline__ uint64_t gl_add_ptx(uint64_t a, uint64_t b) {
   uint64_t r;
-  // s = a + b (carry c); t = s + eps (carry c2). The canonical sum is t when c | c2, else s.
+  // s = a + b (carry c); t = s + eps (carry c2). The canonical sum is t when c | c2, else s. The
+  // carry chains are written as multiply-adds by 1, which run on the integer multiply pipe and
+  // leave the ALU pipe (selects, compares, logic) to the rest of the field and hash code.
   asm("{\n\t"
       ".reg .u32 a0, a1, b0, b1, s0, s1, t0, t1, c, c2;\n\t"
       ".reg .pred p;\n\t"
       "mov.b64 {a0, a1}, %1;\n\t"
       "mov.b64 {b0, b1}, %2;\n\t"
-      "add.cc.u32 s0, a0, b0;\n\t"
-      "addc.cc.u32 s1, a1, b1;\n\t"
+      "mad.lo.cc.u32 s0, a0, 1, b0;\n\t"
+      "madc.lo.cc.u32 s1, a1, 1, b1;\n\t"
       "addc.u32 c, 0, 0;\n\t"
-      "add.cc.u32 t0, s0, 0xffffffff;\n\t"
-      "addc.cc.u32 t1, s1, 0;\n\t"
+      "mad.lo.cc.u32 t0, s0, 1, 0xffffffff;\n\t"
+      "madc.lo.cc.u32 t1, s1, 1, 0;\n\t"
       "addc.u32 c2, 0, 0;\n\t"
       "or.b32 c, c, c2;\n\t"
       "setp.ne.u32 p, c, 0;\n\t"
