@@ -99,16 +99,16 @@ __device__ __forceinline__ uint64_t gl_mul_ptx(uint64_t a, uint64_t b) {
       // y = r2 * (2^32 - 1) as one 32x32 -> 64 multiply (integer multiply pipe)
       "mul.lo.u32 y0, r2, 0xffffffff;\n\t"
       "mul.hi.u32 y1, r2, 0xffffffff;\n\t"
-      // w += y, plus eps on carry
-      "add.cc.u32 r0, r0, y0;\n\t"
-      "addc.cc.u32 r1, r1, y1;\n\t"
+      // w += y, plus eps on carry (carry chains as multiply-adds by 1: integer multiply pipe)
+      "mad.lo.cc.u32 r0, r0, 1, y0;\n\t"
+      "madc.lo.cc.u32 r1, r1, 1, y1;\n\t"
       "addc.u32 c, z, z;\n\t"
-      "sub.u32 c, z, c;\n\t"
-      "add.cc.u32 r0, r0, c;\n\t"
-      "addc.u32 r1, r1, z;\n\t"
+      "mul.lo.u32 c, c, 0xffffffff;\n\t"
+      "mad.lo.cc.u32 r0, r0, 1, c;\n\t"
+      "madc.lo.u32 r1, r1, 1, z;\n\t"
       // canonical: if w + eps carries, w >= p and the result is w + eps mod 2^64
-      "add.cc.u32 t0, r0, 0xffffffff;\n\t"
-      "addc.cc.u32 t1, r1, z;\n\t"
+      "mad.lo.cc.u32 t0, r0, 1, 0xffffffff;\n\t"
+      "madc.lo.cc.u32 t1, r1, 1, z;\n\t"
       "addc.u32 c, z, z;\n\t"
       "setp.ne.u32 p, c, 0;\n\t"
       "selp.b32 r0, t0, r0, p;\n\t"
