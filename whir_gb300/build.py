@@ -13,7 +13,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libwhir_gb300.so")
 SOURCES = ["commit.cu", "commit_mont.cu", "sumcheck.cu", "sumcheck_mont.cu", "prover.cu", "noalloc.cu"]
 HEADERS = ["field.cuh", "hash.cuh", "kernels.hpp", "protocol.hpp", "status.hpp", "roots.cuh", "encode.cuh",
-           "sumcheck.cuh", "sponge.cuh"]
+           "sumcheck.cuh", "sponge.cuh", "wide.cuh"]
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",

@@ -16,6 +16,7 @@
 #include "field.cuh"
 #include "kernels.hpp"
 #include "roots.cuh"
+#include "wide.cuh"
 
 namespace whir {
 
@@ -99,17 +100,20 @@ __device__ void finish_pairs(T acc0, T acc2, T* partials, T* out, unsigned int* 
 template <class T>
 __global__ void __launch_bounds__(SC_THREADS) sc_compute_kernel(const T* a, const T* b, uint64_t n, T* partials,
                                                                  T* out, unsigned int* counter) {
-  T acc0 = T::zero(), acc2 = T::zero();
+  WideAcc<T> w0, w2;
+  w0.init();
+  w2.init();
   if (n == 1) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) acc0 = a[0] * b[0];
+    if (blockIdx.x == 0 && threadIdx.x == 0) w0.mac(a[0], b[0]);
   } else {
     const uint64_t h = n >> 1;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < h; i += (uint64_t)gridDim.x * blockDim.x) {
       const T a0 = a[i], a1 = a[i + h], b0 = b[i], b1 = b[i + h];
-      acc0 += a0 * b0;
-      acc2 += (a1 - a0) * (b1 - b0);
+      w0.mac(a0, b0);
+      w2.mac(a1 - a0, b1 - b0);
     }
   }
+  T acc0 = w0.get(), acc2 = w2.get();
   acc0 = block_sum(acc0);
   acc2 = block_sum(acc2);
   finish_pairs(acc0, acc2, partials, out, counter);
@@ -118,16 +122,18 @@ __global__ void __launch_bounds__(SC_THREADS) sc_compute_kernel(const T* a, cons
 template <class T>
 __global__ void __launch_bounds__(SC_THREADS) sc_fold_compute_kernel(T* a, T* b, uint64_t n, T r, T* partials,
                                                                       T* out, unsigned int* counter) {
-  T acc0 = T::zero(), acc2 = T::zero();
+  WideAcc<T> w0, w2;
+  w0.init();
+  w2.init();
   if (n <= 2) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       if (n == 2) {
         const T fa = a[0] + (a[1] - a[0]) * r, fb = b[0] + (b[1] - b[0]) * r;
         a[0] = fa;
         b[0] = fb;
-        acc0 = fa * fb;
+        w0.mac(fa, fb);
       } else if (n == 1) {
-        acc0 = a[0] * b[0];
+        w0.mac(a[0], b[0]);
       }
     }
   } else {
@@ -141,10 +147,11 @@ __global__ void __launch_bounds__(SC_THREADS) sc_fold_compute_kernel(T* a, T* b,
       a[i + q] = fa1;
       b[i] = fb0;
       b[i + q] = fb1;
-      acc0 += fa0 * fb0;
-      acc2 += (fa1 - fa0) * (fb1 - fb0);
+      w0.mac(fa0, fb0);
+      w2.mac(fa1 - fa0, fb1 - fb0);
     }
   }
+  T acc0 = w0.get(), acc2 = w2.get();
   acc0 = block_sum(acc0);
   acc2 = block_sum(acc2);
   finish_pairs(acc0, acc2, partials, out, counter);
@@ -424,6 +431,101 @@ cudaError_t launch_eq_table(const T* point, int off, int cnt, T scalar, T* table
 // Fused first sumcheck rounds: a = map(x) and b = sum_l rlc_l eq(point_l, .) are evaluated on the
 // fly from the coefficient vector and small eq tables instead of being written to HBM.
 // ---------------------------------------------------------------------------------------------
+// With eq(i) = sum_f hi_f[i >> l] lo_f[i & (2^l - 1)] and the folded (top) variables inside the hi
+// index, every sum of the first two rounds factors into per-row sums of lo-weighted coefficients
+// times one hi-side factor per row (R = 2^(h-1) rows in the half with top bit 0):
+//   round 1: c0 = sum_H sum_f hi_f[H] * S_f(H, x),
+//            c2 = sum_H sum_f (hi_f[H + R] - hi_f[H]) * S_f(H, x_top - x),   S_f(H, y) = sum_j lo_f[j] y[H 2^l + j];
+//   round 2: the folded covector is b'(H 2^l + j) = sum_f lo_f[j] (hi_f[H] + r (hi_f[H + R] - hi_f[H])).
+// Each coefficient then costs one product per form instead of two eq products and a fold. Work is
+// split in units of (row, chunk of EQ_CHUNK columns); each thread multiplies its own partial row sums
+// by the row factor (linearity), so no per-row block reduction is needed.
+static constexpr uint64_t EQ_CHUNK = 2048;
+static constexpr int EQ_MAX_FORMS = 16;
+
+template <class T, class S>
+__global__ void __launch_bounds__(SC_THREADS) first_compute_eq_kernel(const S* x, uint64_t n, const T* tables,
+                                                                      int nforms, int h, int l, T* partials,
+                                                                      T* out, unsigned int* counter) {
+  const uint64_t hs = 1ull << h, ls = 1ull << l, rows = hs >> 1, half = n >> 1;
+  const uint64_t chunk = ls < EQ_CHUNK ? ls : EQ_CHUNK, per_row = ls / chunk, units = rows * per_row;
+  T acc0 = T::zero(), acc2 = T::zero();
+  for (uint64_t u = blockIdx.x; u < units; u += gridDim.x) {
+    const uint64_t H = u / per_row, j0 = (u - H * per_row) * chunk, base = H * ls;
+    for (int f = 0; f < nforms; ++f) {
+      const T* hi = tables + (uint64_t)f * (hs + ls);
+      const T* lo = hi + hs;
+      WideAcc<T> s0, s2;
+      s0.init();
+      s2.init();
+      for (uint64_t j = j0 + threadIdx.x; j < j0 + chunk; j += blockDim.x) {
+        const S x0 = x[base + j], x1 = x[base + half + j];
+        const T w = lo[j];
+        s0.mac_mixed(w, x0);
+        s2.mac_mixed(w, x1 - x0);
+      }
+      const T h0 = hi[H];
+      acc0 += h0 * s0.get();
+      acc2 += (hi[H + rows] - h0) * s2.get();
+    }
+  }
+  acc0 = block_sum(acc0);
+  acc2 = block_sum(acc2);
+  finish_pairs(acc0, acc2, partials, out, counter);
+}
+
+// Round 2 by rows (h >= 2, nforms <= EQ_MAX_FORMS): folds x and the covector with r into a_out /
+// b_out (n/2 each) and computes (c0, c2) of the folded pair; rows H < R/2 pair with rows H + R/2
+// (the second variable is the second bit of the hi index).
+template <class T, class S>
+__global__ void __launch_bounds__(SC_THREADS) first_fold_compute_rows_kernel(const S* x, uint64_t n, T r,
+                                                                            const T* tables, int nforms, int h,
+                                                                            int l, T* a_out, T* b_out,
+                                                                            T* partials, T* out,
+                                                                            unsigned int* counter) {
+  __shared__ T rowf[2][EQ_MAX_FORMS];
+  const uint64_t hs = 1ull << h, ls = 1ull << l, rows = hs >> 1, qr = hs >> 2;
+  const uint64_t q = n >> 2, hf = n >> 1;
+  const uint64_t chunk = ls < EQ_CHUNK ? ls : EQ_CHUNK, per_row = ls / chunk, units = qr * per_row;
+  WideAcc<T> w0, w2;
+  w0.init();
+  w2.init();
+  for (uint64_t u = blockIdx.x; u < units; u += gridDim.x) {
+    const uint64_t H = u / per_row, j0 = (u - H * per_row) * chunk, base = H * ls;
+    __syncthreads();  // the previous unit's readers are done with rowf
+    if (threadIdx.x < 2 * nforms) {
+      const int f = threadIdx.x >> 1, side = threadIdx.x & 1;
+      const T* hi = tables + (uint64_t)f * (hs + ls);
+      const uint64_t R0 = H + side * qr;
+      rowf[side][f] = hi[R0] + r * (hi[R0 + rows] - hi[R0]);
+    }
+    __syncthreads();
+    for (uint64_t j = j0 + threadIdx.x; j < j0 + chunk; j += blockDim.x) {
+      const uint64_t i = base + j;
+      const S x0 = x[i], x1 = x[i + q], x2 = x[i + hf], x3 = x[i + hf + q];
+      const T fa0 = Embed<T, S>::map(x0) + Embed<T, S>::mul(r, x2 - x0);
+      const T fa1 = Embed<T, S>::map(x1) + Embed<T, S>::mul(r, x3 - x1);
+      T fb0 = T::zero(), fb1 = T::zero();
+      for (int f = 0; f < nforms; ++f) {
+        const T w = tables[(uint64_t)f * (hs + ls) + hs + j];
+        fb0 += w * rowf[0][f];
+        fb1 += w * rowf[1][f];
+      }
+      a_out[i] = fa0;
+      a_out[i + q] = fa1;
+      b_out[i] = fb0;
+      b_out[i + q] = fb1;
+      w0.mac(fa0, fb0);
+      w2.mac(fa1 - fa0, fb1 - fb0);
+    }
+  }
+  T acc0 = w0.get(), acc2 = w2.get();
+  acc0 = block_sum(acc0);
+  acc2 = block_sum(acc2);
+  finish_pairs(acc0, acc2, partials, out, counter);
+}
+
+// eq evaluated at one index (round 2 for small shapes or many forms, and the MLE dot product).
 template <class T>
 __device__ __forceinline__ T eq_on_the_fly(const T* tables, int nforms, int h, int l, uint64_t i) {
   const uint64_t hs = 1ull << h, ls = 1ull << l;
@@ -436,28 +538,13 @@ __device__ __forceinline__ T eq_on_the_fly(const T* tables, int nforms, int h, i
 }
 
 template <class T, class S>
-__global__ void __launch_bounds__(SC_THREADS) first_compute_eq_kernel(const S* x, uint64_t n, const T* tables,
-                                                                      int nforms, int h, int l, T* partials,
-                                                                      T* out, unsigned int* counter) {
-  T acc0 = T::zero(), acc2 = T::zero();
-  const uint64_t half = n >> 1;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < half; i += (uint64_t)gridDim.x * blockDim.x) {
-    const S x0 = x[i], x1 = x[i + half];
-    const T b0 = eq_on_the_fly(tables, nforms, h, l, i), b1 = eq_on_the_fly(tables, nforms, h, l, i + half);
-    acc0 += Embed<T, S>::mul(b0, x0);
-    acc2 += Embed<T, S>::mul(b1 - b0, x1 - x0);
-  }
-  acc0 = block_sum(acc0);
-  acc2 = block_sum(acc2);
-  finish_pairs(acc0, acc2, partials, out, counter);
-}
-
-template <class T, class S>
 __global__ void __launch_bounds__(SC_THREADS) first_fold_compute_eq_kernel(const S* x, uint64_t n, T r,
                                                                            const T* tables, int nforms, int h, int l,
                                                                            T* a_out, T* b_out, T* partials, T* out,
                                                                            unsigned int* counter) {
-  T acc0 = T::zero(), acc2 = T::zero();
+  WideAcc<T> w0, w2;
+  w0.init();
+  w2.init();
   const uint64_t q = n >> 2, hf = n >> 1;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < q; i += (uint64_t)gridDim.x * blockDim.x) {
     const S x0 = x[i], x1 = x[i + q], x2 = x[i + hf], x3 = x[i + hf + q];
@@ -470,9 +557,10 @@ __global__ void __launch_bounds__(SC_THREADS) first_fold_compute_eq_kernel(const
     a_out[i + q] = fa1;
     b_out[i] = fb0;
     b_out[i + q] = fb1;
-    acc0 += fa0 * fb0;
-    acc2 += (fa1 - fa0) * (fb1 - fb0);
+    w0.mac(fa0, fb0);
+    w2.mac(fa1 - fa0, fb1 - fb0);
   }
+  T acc0 = w0.get(), acc2 = w2.get();
   acc0 = block_sum(acc0);
   acc2 = block_sum(acc2);
   finish_pairs(acc0, acc2, partials, out, counter);
@@ -481,7 +569,14 @@ __global__ void __launch_bounds__(SC_THREADS) first_fold_compute_eq_kernel(const
 template <class T, class S>
 cudaError_t launch_first_compute_eq(const S* x, size_t n, const T* tables, int nforms, int nv, T* partials,
                                     size_t* nparts, cudaStream_t s, T* out, unsigned int* counter) {
+  if (nv < 2 || n != (1ull << nv)) return cudaErrorInvalidValue;  // the row split needs h >= 1
   size_t g = sumcheck_partials(n);
+  {
+    const int h = nv / 2, l = nv - nv / 2;
+    const uint64_t ls = 1ull << l, chunk = std::min<uint64_t>(ls, EQ_CHUNK);
+    const uint64_t units = (1ull << (h - 1)) * (ls / chunk);
+    g = std::max<size_t>(1, std::min<size_t>(g, units));
+  }
   first_compute_eq_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(x, n, tables, nforms, nv / 2, nv - nv / 2,
                                                                     partials, out, counter);
   note_launch();
@@ -493,9 +588,17 @@ cudaError_t launch_first_fold_compute_eq(const S* x, size_t n, T r, const T* tab
                                          T* b_out, T* partials, size_t* nparts, cudaStream_t s, T* out,
                                          unsigned int* counter) {
   size_t g = sumcheck_partials(n);
-  first_fold_compute_eq_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(x, n, r, tables, nforms, nv / 2,
-                                                                         nv - nv / 2, a_out, b_out, partials, out,
-                                                                         counter);
+  const int h = nv / 2, l = nv - nv / 2;
+  if (h >= 2 && nforms <= EQ_MAX_FORMS && n == (1ull << nv)) {
+    const uint64_t ls = 1ull << l, chunk = std::min<uint64_t>(ls, EQ_CHUNK);
+    const uint64_t units = (1ull << (h - 2)) * (ls / chunk);
+    g = std::max<size_t>(1, std::min<size_t>(g, units));
+    first_fold_compute_rows_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(x, n, r, tables, nforms, h, l, a_out,
+                                                                             b_out, partials, out, counter);
+  } else {
+    first_fold_compute_eq_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(x, n, r, tables, nforms, h, l, a_out,
+                                                                           b_out, partials, out, counter);
+  }
   note_launch();
   *nparts = g;
   return cudaGetLastError();
