@@ -131,6 +131,18 @@ template <class T, class S>
 cudaError_t launch_first_fold_compute_eq(const S* x, size_t n, T r, const T* tables, int nforms, int nv, T* a_out,
                                          T* b_out, T* partials, size_t* nparts, cudaStream_t s, T* out = nullptr,
                                          unsigned int* counter = nullptr);
+// Row-factored rounds of the fused initial sumcheck (n = 2^nv, h = nv/2, l = nv - h): the covector
+// is sum_f lo_f[j] F_f[H] at index H 2^l + j, with row factors F (2^rlog rows, per-form stride
+// fstride; the hi tables at first). Folds a_in (length m = 2^(rlog + l)) with r into a_out (m/2; may
+// be a_in), folds F into F_next (per-form stride 2^h), and computes (c0, c2) of the folded pair.
+template <class T, class S>
+cudaError_t launch_rows_fold_compute(const S* a_in, size_t m, T r, const T* F, size_t fstride, int rlog,
+                                     const T* tables, int nforms, int nv, T* a_out, T* F_next, T* partials,
+                                     size_t* nparts, cudaStream_t s, T* out = nullptr, unsigned int* counter = nullptr);
+// Folds a (length m) with r in place and writes the folded covector (m/2 values) from row factors F.
+template <class T>
+cudaError_t launch_rows_finish(T* a, size_t m, T r, const T* F, int rlog, const T* tables, int nforms, int nv,
+                               T* b_out, cudaStream_t s);
 // sum_i map(x_i) * eq(point, i) for n <= 2^nv (implicit zero padding), from one eq table pair
 // (hi: 2^(nv/2) entries, then lo: 2^(nv - nv/2)); block sums -> partials (reduce_singles).
 template <class T, class S>

@@ -543,6 +543,60 @@ std::vector<T> initial_sumcheck_fused(whir_ctx* ctx, const Sumcheck& c, Transcri
   std::vector<T> rs;
   SumcheckBuffers<T> buf(ctx, n);
   T prev = T::zero();
+  // Prover round messages and challenges (protocols/sumcheck.rs:104-155) once (c0, c2) is in buf.out.
+  auto transcript_round = [&]() {
+    T cc[2];
+    d2h(ctx, cc, buf.out.p, sizeof(cc));
+    const T c0 = cc[0], c2 = cc[1];
+    const T c1 = sum - c0.dbl() - c2;
+    send_elem<T>(ts, c0);
+    send_elem<T>(ts, c2);
+    pow_prove(ctx, c.round_pow, ts);
+    T r = challenge<T>(ts);
+    rs.push_back(r);
+    sum = (c2 * r + c1) * r + c0;
+    prev = r;
+  };
+  if (c.num_rounds >= 2 && (int)c.num_rounds <= nvars / 2 && nforms <= 16 && n == ((size_t)1 << nvars)) {
+    // Every folded variable lies in the hi index of the eq tables: the covector stays factored as
+    // lo x row factors (only the factors are folded) and is written once, after the last round.
+    const int h = nvars / 2, l = nvars - h;
+    const size_t hs = (size_t)1 << h;
+    DBuf<T> fb(ctx, 2 * (size_t)nforms * hs);
+    const T* F = tables;
+    size_t fstride = hs + ((size_t)1 << l), m = n;
+    int rlog = h;
+    for (size_t round = 0; round < c.num_rounds; ++round) {
+      size_t np = 0;
+      {
+        ProfScope prof(ctx, PF_SUMCHECK);
+        if (round == 0) {
+          CU((launch_first_compute_eq<T, S>(x, n, tables, nforms, nvars, buf.parts.p, &np, ctx->stream, buf.out.p,
+                                            buf.counter.p)));
+        } else {
+          T* Fn = fb.p + (round & 1) * (size_t)nforms * hs;
+          if (round == 1) {
+            CU((launch_rows_fold_compute<T, S>(x, m, prev, F, fstride, rlog, tables, nforms, nvars, a, Fn,
+                                               buf.parts.p, &np, ctx->stream, buf.out.p, buf.counter.p)));
+          } else {
+            CU((launch_rows_fold_compute<T, T>(a, m, prev, F, fstride, rlog, tables, nforms, nvars, a, Fn,
+                                               buf.parts.p, &np, ctx->stream, buf.out.p, buf.counter.p)));
+          }
+          F = Fn;
+          fstride = hs;
+          rlog -= 1;
+          m /= 2;
+        }
+      }
+      transcript_round();
+    }
+    {
+      ProfScope prof(ctx, PF_SUMCHECK);
+      CU(launch_rows_finish<T>(a, m, prev, F, rlog, tables, nforms, nvars, b, ctx->stream));
+    }
+    n = m / 2;
+    return rs;
+  }
   for (size_t round = 0; round < c.num_rounds; ++round) {
     size_t np = 0;
     {
@@ -559,17 +613,7 @@ std::vector<T> initial_sumcheck_fused(whir_ctx* ctx, const Sumcheck& c, Transcri
         n = n > 1 ? n / 2 : n;
       }
     }
-    T cc[2];
-    d2h(ctx, cc, buf.out.p, sizeof(cc));
-    const T c0 = cc[0], c2 = cc[1];
-    const T c1 = sum - c0.dbl() - c2;
-    send_elem<T>(ts, c0);
-    send_elem<T>(ts, c2);
-    pow_prove(ctx, c.round_pow, ts);
-    T r = challenge<T>(ts);
-    rs.push_back(r);
-    sum = (c2 * r + c1) * r + c0;
-    prev = r;
+    transcript_round();
   }
   {
     ProfScope prof(ctx, PF_SUMCHECK);

@@ -19,5 +19,11 @@ template cudaError_t launch_lift_rlc<Gl2, Gl2>(Gl2*, const Gl2* const*, const Gl
 template cudaError_t launch_lift_rlc<Gl3, Gl3>(Gl3*, const Gl3* const*, const Gl3*, size_t, size_t, cudaStream_t);
 template cudaError_t launch_univariate_eval<Gl2, Gl2>(const Gl2*, size_t, Gl2, Gl2*, size_t*, cudaStream_t);
 template cudaError_t launch_univariate_eval<Gl3, Gl3>(const Gl3*, size_t, Gl3, Gl3*, size_t*, cudaStream_t);
+template cudaError_t launch_rows_fold_compute<Gl2, Gl2>(const Gl2*, size_t, Gl2, const Gl2*, size_t, int, const Gl2*,
+                                                        int, int, Gl2*, Gl2*, Gl2*, size_t*, cudaStream_t, Gl2*,
+                                                        unsigned int*);
+template cudaError_t launch_rows_fold_compute<Gl3, Gl3>(const Gl3*, size_t, Gl3, const Gl3*, size_t, int, const Gl3*,
+                                                        int, int, Gl3*, Gl3*, Gl3*, size_t*, cudaStream_t, Gl3*,
+                                                        unsigned int*);
 
 }  // namespace whir

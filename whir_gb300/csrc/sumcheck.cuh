@@ -566,6 +566,89 @@ __global__ void __launch_bounds__(SC_THREADS) first_fold_compute_eq_kernel(const
   finish_pairs(acc0, acc2, partials, out, counter);
 }
 
+// Later rounds of the fused initial sumcheck while the folded variables stay inside the hi index:
+// the covector keeps the form b(H 2^l + j) = sum_f lo_f[j] F_f[H] with row factors F (F = hi for
+// the unfolded covector), so folding it only folds F, and b is never written. One launch folds
+// a_in (length m) with r into a_out (m/2, may alias a_in), folds F (2^rlog rows, per-form stride
+// fstride) into F_next (per-form stride 2^h), and computes (c0, c2) of the next round from
+// row sums of lo-weighted a values. Needs rlog >= 2 and nforms <= EQ_MAX_FORMS.
+template <class T, class S>
+__global__ void __launch_bounds__(SC_THREADS) rows_fold_compute_kernel(const S* a_in, uint64_t m, T r, const T* F,
+                                                                      uint64_t fstride, int rlog, const T* tables,
+                                                                      int nforms, int h, int l, T* a_out,
+                                                                      T* F_next, T* partials, T* out,
+                                                                      unsigned int* counter) {
+  __shared__ T rowf[2][EQ_MAX_FORMS];
+  const uint64_t hs = 1ull << h, ls = 1ull << l;
+  const uint64_t half_rows = (1ull << rlog) >> 1, qr = (1ull << rlog) >> 2;
+  const uint64_t hf = m >> 1, q = m >> 2;
+  const uint64_t chunk = ls < EQ_CHUNK ? ls : EQ_CHUNK, per_row = ls / chunk, units = qr * per_row;
+  T acc0 = T::zero(), acc2 = T::zero();
+  for (uint64_t u = blockIdx.x; u < units; u += gridDim.x) {
+    const uint64_t H = u / per_row, j0 = (u - H * per_row) * chunk, base = H * ls;
+    __syncthreads();  // the previous unit's readers are done with rowf
+    if (threadIdx.x < 2 * nforms) {
+      const int f = threadIdx.x >> 1, side = threadIdx.x & 1;
+      const T* Ff = F + (uint64_t)f * fstride;
+      const uint64_t R0 = H + side * qr;
+      const T v = Ff[R0] + r * (Ff[R0 + half_rows] - Ff[R0]);
+      rowf[side][f] = v;
+      if (j0 == 0) F_next[(uint64_t)f * hs + R0] = v;
+    }
+    __syncthreads();
+    for (int f = 0; f < nforms; ++f) {
+      const T* lo = tables + (uint64_t)f * (hs + ls) + hs;
+      WideAcc<T> s0, s2;
+      s0.init();
+      s2.init();
+      for (uint64_t j = j0 + threadIdx.x; j < j0 + chunk; j += blockDim.x) {
+        const uint64_t i = base + j;
+        T fa0, fa1;
+        if (f == 0) {
+          const S x0 = a_in[i], x1 = a_in[i + q], x2 = a_in[i + hf], x3 = a_in[i + hf + q];
+          fa0 = Embed<T, S>::map(x0) + Embed<T, S>::mul(r, x2 - x0);
+          fa1 = Embed<T, S>::map(x1) + Embed<T, S>::mul(r, x3 - x1);
+          a_out[i] = fa0;
+          a_out[i + q] = fa1;
+        } else {
+          fa0 = a_out[i];  // written by this thread in the first pass
+          fa1 = a_out[i + q];
+        }
+        const T w = lo[j];
+        s0.mac(w, fa0);
+        s2.mac(w, fa1 - fa0);
+      }
+      acc0 += rowf[0][f] * s0.get();
+      acc2 += (rowf[1][f] - rowf[0][f]) * s2.get();
+    }
+  }
+  acc0 = block_sum(acc0);
+  acc2 = block_sum(acc2);
+  finish_pairs(acc0, acc2, partials, out, counter);
+}
+
+// End of the row-factored rounds: folds a (length m) with r in place and writes the folded
+// covector b_out[i] = sum_f lo_f[j] (F_f[H] + r (F_f[H + R/2] - F_f[H])), i = H 2^l + j < m/2,
+// from row factors F with R = 2^rlog rows (per-form stride 2^h).
+template <class T>
+__global__ void __launch_bounds__(SC_THREADS) rows_finish_kernel(T* a, uint64_t m, T r, const T* F, int rlog,
+                                                                 const T* tables, int nforms, int h, int l,
+                                                                 T* b_out) {
+  const uint64_t hs = 1ull << h, ls = 1ull << l, half_rows = (1ull << rlog) >> 1, hf = m >> 1;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < hf; i += (uint64_t)gridDim.x * blockDim.x) {
+    const T lo = a[i], hi = a[i + hf];
+    a[i] = lo + (hi - lo) * r;
+    const uint64_t H = i >> l, j = i & (ls - 1);
+    T v = T::zero();
+    for (int f = 0; f < nforms; ++f) {
+      const T* Ff = F + (uint64_t)f * hs;
+      const T g = Ff[H] + r * (Ff[H + half_rows] - Ff[H]);
+      v += tables[(uint64_t)f * (hs + ls) + hs + j] * g;
+    }
+    b_out[i] = v;
+  }
+}
+
 template <class T, class S>
 cudaError_t launch_first_compute_eq(const S* x, size_t n, const T* tables, int nforms, int nv, T* partials,
                                     size_t* nparts, cudaStream_t s, T* out, unsigned int* counter) {
@@ -601,6 +684,32 @@ cudaError_t launch_first_fold_compute_eq(const S* x, size_t n, T r, const T* tab
   }
   note_launch();
   *nparts = g;
+  return cudaGetLastError();
+}
+
+template <class T, class S>
+cudaError_t launch_rows_fold_compute(const S* a_in, size_t m, T r, const T* F, size_t fstride, int rlog,
+                                     const T* tables, int nforms, int nv, T* a_out, T* F_next, T* partials,
+                                     size_t* nparts, cudaStream_t s, T* out, unsigned int* counter) {
+  const int h = nv / 2, l = nv - nv / 2;
+  if (rlog < 2 || rlog > h || nforms > EQ_MAX_FORMS || m != ((size_t)1 << (rlog + l))) return cudaErrorInvalidValue;
+  const uint64_t ls = 1ull << l, chunk = std::min<uint64_t>(ls, EQ_CHUNK);
+  const uint64_t units = (1ull << (rlog - 2)) * (ls / chunk);
+  size_t g = std::max<size_t>(1, std::min<size_t>(sumcheck_partials(m), units));
+  rows_fold_compute_kernel<T, S><<<(unsigned)g, SC_THREADS, 0, s>>>(a_in, m, r, F, fstride, rlog, tables, nforms, h, l,
+                                                                     a_out, F_next, partials, out, counter);
+  note_launch();
+  *nparts = g;
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_rows_finish(T* a, size_t m, T r, const T* F, int rlog, const T* tables, int nforms, int nv,
+                               T* b_out, cudaStream_t s) {
+  const int h = nv / 2, l = nv - nv / 2;
+  if (rlog < 1 || rlog > h || m != ((size_t)1 << (rlog + l))) return cudaErrorInvalidValue;
+  const size_t g = std::max<size_t>(1, std::min(SC_MAX_BLOCKS, (m / 2 + SC_THREADS - 1) / SC_THREADS));
+  rows_finish_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(a, m, r, F, rlog, tables, nforms, h, l, b_out);
+  note_launch();
   return cudaGetLastError();
 }
 
@@ -698,7 +807,8 @@ cudaError_t launch_univariate_eval(const S* coeffs, size_t n, T x, T* partials, 
                                                  cudaStream_t);                                                  \
   template cudaError_t launch_scatter<T>(T*, const uint64_t*, const T*, size_t, cudaStream_t);                   \
   template cudaError_t launch_add<T>(T*, const T*, size_t, cudaStream_t);                                        \
-  template cudaError_t launch_eq_table<T>(const T*, int, int, T, T*, cudaStream_t);
+  template cudaError_t launch_eq_table<T>(const T*, int, int, T, T*, cudaStream_t);                              \
+  template cudaError_t launch_rows_finish<T>(T*, size_t, T, const T*, int, const T*, int, int, T*, cudaStream_t);
 
 // Kernels that read coefficient vectors over S and compute over T.
 #define WHIR_SC_EMBED_INST(T, S)                                                                                 \
@@ -708,6 +818,8 @@ cudaError_t launch_univariate_eval(const S* coeffs, size_t n, T x, T* partials, 
                                                           size_t*, cudaStream_t, T*, unsigned int*);             \
   template cudaError_t launch_mle_dot<T, S>(const S*, size_t, const T*, int, T*, size_t*, cudaStream_t);         \
   template cudaError_t launch_lift_rlc<T, S>(T*, const S* const*, const T*, size_t, size_t, cudaStream_t);       \
-  template cudaError_t launch_univariate_eval<T, S>(const S*, size_t, T, T*, size_t*, cudaStream_t);
+  template cudaError_t launch_univariate_eval<T, S>(const S*, size_t, T, T*, size_t*, cudaStream_t);             \
+  template cudaError_t launch_rows_fold_compute<T, S>(const S*, size_t, T, const T*, size_t, int, const T*, int,  \
+                                                      int, T*, T*, T*, size_t*, cudaStream_t, T*, unsigned int*);
 
 }  // namespace whir
