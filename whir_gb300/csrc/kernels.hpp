@@ -80,9 +80,11 @@ cudaError_t launch_gather_digests(const uint32_t* nodes, const uint64_t* idx, si
 // Number of partial (c0, c2) pairs written by the reduce kernels for a vector of n elements.
 size_t sumcheck_partials(size_t n);
 
-// The (c0, c2) kernels below write one partial pair per block. When `counter` is non-null (a zeroed
-// u32 on the device) the last block also sums the partials into out[0..2) and re-zeroes the
-// counter, so no separate reduce launch is needed.
+// The (c0, c2) kernels below write one partial pair per block. When `counter` is non-null (two
+// zeroed u32 on the device: arrival count, launch sequence) the last block also sums the partials
+// into out[0..2), re-zeroes the arrival count and publishes the pair: it increments the sequence
+// and stores it as a u32 right after out[1] (out needs room for it) once the values are visible
+// system-wide, so `out` can be host-mapped memory that the host polls.
 // (c0, c2) of vectors a, b of n = 2^k elements -> partials (2 elements per block)
 template <class T>
 cudaError_t launch_sumcheck_compute(const T* a, const T* b, size_t n, T* partials, size_t* nparts, cudaStream_t s,

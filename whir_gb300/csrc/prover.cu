@@ -7,6 +7,7 @@
 // the final (constant-size) vector.
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -56,6 +57,9 @@ struct whir_ctx {
   uint8_t* h_up = nullptr;  // pinned upload arena (see h2d)
   size_t up_cap = 0, up_off = 0;
   unsigned long long* d_pow = nullptr;
+  // Host-mapped pinned words the round kernels publish their (c0, c2) into (see wait_pair).
+  uint8_t* mail_h = nullptr;
+  uint8_t* mail_d = nullptr;
   uint64_t launches_at_create = 0;
   uint64_t h2d_bytes = 0, d2h_bytes = 0;
   // profiling: event pairs recorded around each kernel family on the context's stream
@@ -479,13 +483,45 @@ void irs_open(whir_ctx* ctx, const Irs& c, Transcript& ts, const std::vector<con
 // ------------------------------------------------------------------------------------------------
 // Sumcheck on the device (protocols/sumcheck.rs:69-162), mask_length == 0.
 // ------------------------------------------------------------------------------------------------
+// Round-message buffers: per-block partials, the last-block counter pair (arrival count, launch
+// sequence) and the output pair, which lives in the context's host-mapped mail words: the kernel's
+// last block writes (c0, c2) there and then the launch sequence, and the host polls that word
+// (wait_pair) instead of issuing a copy and synchronising the stream.
 template <class T>
 struct SumcheckBuffers {
-  DBuf<T> parts, out;
-  DBuf<unsigned int> counter;  // last-block reduction counter (kept at zero between launches)
-  SumcheckBuffers(whir_ctx* ctx, size_t n)
-      : parts(ctx, 2 * sumcheck_partials(n) + 2), out(ctx, 2), counter(ctx, 1) {
-    CU(cudaMemsetAsync(counter.p, 0, sizeof(unsigned int), ctx->stream));
+  whir_ctx* ctx;
+  DBuf<T> parts;
+  DBuf<unsigned int> counter;
+  T* out;    // device alias of the mail words
+  T* out_h;  // host view
+  unsigned int launches = 0;
+  SumcheckBuffers(whir_ctx* c, size_t n) : ctx(c), parts(c, 2 * sumcheck_partials(n) + 2), counter(c, 2) {
+    CU(cudaMemsetAsync(counter.p, 0, 2 * sizeof(unsigned int), ctx->stream));
+    out = reinterpret_cast<T*>(ctx->mail_d);
+    out_h = reinterpret_cast<T*>(ctx->mail_h);
+  }
+  unsigned int* flag_h() { return reinterpret_cast<unsigned int*>(out_h + 2); }
+  // Call before launching a round kernel that publishes into `out`.
+  void arm() {
+    __atomic_store_n(flag_h(), 0u, __ATOMIC_RELEASE);
+    ++launches;
+  }
+  // Waits (bounded) for the armed launch's publication and copies (c0, c2).
+  void wait_pair(T cc[2]) {
+    const auto t0 = std::chrono::steady_clock::now();
+    for (uint64_t spin = 0;; ++spin) {
+      if (__atomic_load_n(flag_h(), __ATOMIC_ACQUIRE) == launches) break;
+      if ((spin & 1023) == 1023) {
+        cudaError_t e = cudaStreamQuery(ctx->stream);
+        if (e != cudaSuccess && e != cudaErrorNotReady) throw Error(WHIR_ERR_CUDA, cudaGetErrorString(e));
+        if (e == cudaSuccess && __atomic_load_n(flag_h(), __ATOMIC_ACQUIRE) != launches)
+          throw Error(WHIR_ERR_INTERNAL, "round kernel finished without publishing its message");
+        if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(60))
+          throw Error(WHIR_ERR_CUDA, "timed out waiting for a sumcheck round");
+      }
+    }
+    memcpy(cc, out_h, 2 * sizeof(T));
+    ctx->d2h_bytes += 2 * sizeof(T);
   }
 };
 
@@ -502,15 +538,16 @@ std::vector<T> sumcheck_device(whir_ctx* ctx, const Sumcheck& c, Transcript& ts,
     size_t np = 0;
     {
       ProfScope prof(ctx, PF_SUMCHECK);
+      buf.arm();
       if (!have) {
-        CU(launch_sumcheck_compute<T>(a, b, n, buf.parts.p, &np, ctx->stream, buf.out.p, buf.counter.p));
+        CU(launch_sumcheck_compute<T>(a, b, n, buf.parts.p, &np, ctx->stream, buf.out, buf.counter.p));
       } else {
-        CU(launch_fold_compute<T>(a, b, n, prev, buf.parts.p, &np, ctx->stream, buf.out.p, buf.counter.p));
+        CU(launch_fold_compute<T>(a, b, n, prev, buf.parts.p, &np, ctx->stream, buf.out, buf.counter.p));
         n = n > 1 ? n / 2 : n;
       }
     }
     T cc[2];
-    d2h(ctx, cc, buf.out.p, sizeof(cc));
+    buf.wait_pair(cc);
     const T c0 = cc[0], c2 = cc[1];
     const T c1 = sum - c0.dbl() - c2;
     send_elem<T>(ts, c0);
@@ -546,7 +583,7 @@ std::vector<T> initial_sumcheck_fused(whir_ctx* ctx, const Sumcheck& c, Transcri
   // Prover round messages and challenges (protocols/sumcheck.rs:104-155) once (c0, c2) is in buf.out.
   auto transcript_round = [&]() {
     T cc[2];
-    d2h(ctx, cc, buf.out.p, sizeof(cc));
+    buf.wait_pair(cc);
     const T c0 = cc[0], c2 = cc[1];
     const T c1 = sum - c0.dbl() - c2;
     send_elem<T>(ts, c0);
@@ -570,17 +607,18 @@ std::vector<T> initial_sumcheck_fused(whir_ctx* ctx, const Sumcheck& c, Transcri
       size_t np = 0;
       {
         ProfScope prof(ctx, PF_SUMCHECK);
+        buf.arm();
         if (round == 0) {
-          CU((launch_first_compute_eq<T, S>(x, n, tables, nforms, nvars, buf.parts.p, &np, ctx->stream, buf.out.p,
+          CU((launch_first_compute_eq<T, S>(x, n, tables, nforms, nvars, buf.parts.p, &np, ctx->stream, buf.out,
                                             buf.counter.p)));
         } else {
           T* Fn = fb.p + (round & 1) * (size_t)nforms * hs;
           if (round == 1) {
             CU((launch_rows_fold_compute<T, S>(x, m, prev, F, fstride, rlog, tables, nforms, nvars, a, Fn,
-                                               buf.parts.p, &np, ctx->stream, buf.out.p, buf.counter.p)));
+                                               buf.parts.p, &np, ctx->stream, buf.out, buf.counter.p)));
           } else {
             CU((launch_rows_fold_compute<T, T>(a, m, prev, F, fstride, rlog, tables, nforms, nvars, a, Fn,
-                                               buf.parts.p, &np, ctx->stream, buf.out.p, buf.counter.p)));
+                                               buf.parts.p, &np, ctx->stream, buf.out, buf.counter.p)));
           }
           F = Fn;
           fstride = hs;
@@ -601,15 +639,16 @@ std::vector<T> initial_sumcheck_fused(whir_ctx* ctx, const Sumcheck& c, Transcri
     size_t np = 0;
     {
       ProfScope prof(ctx, PF_SUMCHECK);
+      buf.arm();
       if (round == 0) {
-        CU((launch_first_compute_eq<T, S>(x, n, tables, nforms, nvars, buf.parts.p, &np, ctx->stream, buf.out.p,
+        CU((launch_first_compute_eq<T, S>(x, n, tables, nforms, nvars, buf.parts.p, &np, ctx->stream, buf.out,
                                           buf.counter.p)));
       } else if (round == 1) {
         CU((launch_first_fold_compute_eq<T, S>(x, n, prev, tables, nforms, nvars, a, b, buf.parts.p, &np,
-                                               ctx->stream, buf.out.p, buf.counter.p)));
+                                               ctx->stream, buf.out, buf.counter.p)));
         n /= 2;
       } else {
-        CU(launch_fold_compute<T>(a, b, n, prev, buf.parts.p, &np, ctx->stream, buf.out.p, buf.counter.p));
+        CU(launch_fold_compute<T>(a, b, n, prev, buf.parts.p, &np, ctx->stream, buf.out, buf.counter.p));
         n = n > 1 ? n / 2 : n;
       }
     }
@@ -1054,6 +1093,9 @@ int whir_ctx_create(int device, whir_ctx** out) {
     CU(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
     root_tab<Gl>(ctx.get());  // the other fields' tables are built on first use
     CU(cudaMalloc((void**)&ctx->d_pow, 2 * sizeof(unsigned long long)));
+    CU(cudaHostAlloc((void**)&ctx->mail_h, 4096, cudaHostAllocMapped));
+    memset(ctx->mail_h, 0, 4096);
+    CU(cudaHostGetDevicePointer((void**)&ctx->mail_d, ctx->mail_h, 0));
     stage_reserve(ctx.get(), 1 << 20);
     ctx->up_cap = 8 << 20;
     CU(cudaMallocHost((void**)&ctx->h_up, ctx->up_cap));
@@ -1077,6 +1119,7 @@ int whir_ctx_destroy(whir_ctx* ctx) {
   if (ctx->d_pow) cudaFree(ctx->d_pow);
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
   if (ctx->h_up) cudaFreeHost(ctx->h_up);
+  if (ctx->mail_h) cudaFreeHost(ctx->mail_h);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return 0;

@@ -55,6 +55,28 @@ __device__ T block_sum(T x) {
   return x;
 }
 
+// Two block-wide sums in one pass (one pair of barriers); the results are valid in thread 0.
+template <class T>
+__device__ void block_sum2(T& a, T& b) {
+  __shared__ T part[2][32];
+  a = warp_sum(a);
+  b = warp_sum(b);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    part[0][warp] = a;
+    part[1][warp] = b;
+  }
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  a = (threadIdx.x < nw) ? part[0][threadIdx.x] : T::zero();
+  b = (threadIdx.x < nw) ? part[1][threadIdx.x] : T::zero();
+  if (warp == 0) {
+    a = warp_sum(a);
+    b = warp_sum(b);
+  }
+  __syncthreads();
+}
+
 template <class T>
 __device__ __forceinline__ T ldcg_t(const T* p) {
   T r;
@@ -65,11 +87,37 @@ __device__ __forceinline__ T ldcg_t(const T* p) {
   return r;
 }
 
-// Stores this block's (c0, c2) partial. With a counter, the last block to finish also sums all
-// partials into out[0..2) and re-arms the counter, so one launch yields the round message.
+// Publishes a round message written to out[0..2): bumps the launch sequence counter[1] and stores it
+// in the word after out[1] once the values are visible system-wide. `out` may be host-mapped
+// memory, which the host polls instead of copying and synchronising the stream.
+template <class T>
+__device__ __forceinline__ void publish_pair(T* out, unsigned int* counter) {
+  const unsigned int seq = counter[1] + 1;
+  counter[1] = seq;
+  __threadfence_system();
+  *reinterpret_cast<volatile unsigned int*>(out + 2) = seq;
+}
+
+// Sums the block's per-thread (c0, c2) accumulators and stores the block partial. With a counter,
+// the last block to finish also sums all partials into out[0..2), re-arms counter[0] and publishes
+// the pair (publish_pair), so one launch yields the round message. A one-block launch writes out
+// directly.
 template <class T>
 __device__ void finish_pairs(T acc0, T acc2, T* partials, T* out, unsigned int* counter) {
+  block_sum2(acc0, acc2);
   __shared__ bool am_last;
+  if (gridDim.x == 1) {
+    if (threadIdx.x == 0) {
+      partials[0] = acc0;
+      partials[1] = acc2;
+      if (out) {
+        out[0] = acc0;
+        out[1] = acc2;
+        if (counter) publish_pair(out, counter);
+      }
+    }
+    return;
+  }
   if (threadIdx.x == 0) {
     partials[2 * blockIdx.x] = acc0;
     partials[2 * blockIdx.x + 1] = acc2;
@@ -87,15 +135,14 @@ __device__ void finish_pairs(T acc0, T acc2, T* partials, T* out, unsigned int* 
     s0 += ldcg_t(partials + 2 * i);
     s2 += ldcg_t(partials + 2 * i + 1);
   }
-  s0 = block_sum(s0);
-  s2 = block_sum(s2);
+  block_sum2(s0, s2);
   if (threadIdx.x == 0) {
     out[0] = s0;
     out[1] = s2;
-    *counter = 0;
+    counter[0] = 0;
+    publish_pair(out, counter);
   }
 }
-
 
 template <class T>
 __global__ void __launch_bounds__(SC_THREADS) sc_compute_kernel(const T* a, const T* b, uint64_t n, T* partials,
@@ -114,8 +161,6 @@ __global__ void __launch_bounds__(SC_THREADS) sc_compute_kernel(const T* a, cons
     }
   }
   T acc0 = w0.get(), acc2 = w2.get();
-  acc0 = block_sum(acc0);
-  acc2 = block_sum(acc2);
   finish_pairs(acc0, acc2, partials, out, counter);
 }
 
@@ -152,8 +197,6 @@ __global__ void __launch_bounds__(SC_THREADS) sc_fold_compute_kernel(T* a, T* b,
     }
   }
   T acc0 = w0.get(), acc2 = w2.get();
-  acc0 = block_sum(acc0);
-  acc2 = block_sum(acc2);
   finish_pairs(acc0, acc2, partials, out, counter);
 }
 
@@ -469,8 +512,6 @@ __global__ void __launch_bounds__(SC_THREADS) first_compute_eq_kernel(const S* x
       acc2 += (hi[H + rows] - h0) * s2.get();
     }
   }
-  acc0 = block_sum(acc0);
-  acc2 = block_sum(acc2);
   finish_pairs(acc0, acc2, partials, out, counter);
 }
 
@@ -520,8 +561,6 @@ __global__ void __launch_bounds__(SC_THREADS) first_fold_compute_rows_kernel(con
     }
   }
   T acc0 = w0.get(), acc2 = w2.get();
-  acc0 = block_sum(acc0);
-  acc2 = block_sum(acc2);
   finish_pairs(acc0, acc2, partials, out, counter);
 }
 
@@ -561,8 +600,6 @@ __global__ void __launch_bounds__(SC_THREADS) first_fold_compute_eq_kernel(const
     w2.mac(fa1 - fa0, fb1 - fb0);
   }
   T acc0 = w0.get(), acc2 = w2.get();
-  acc0 = block_sum(acc0);
-  acc2 = block_sum(acc2);
   finish_pairs(acc0, acc2, partials, out, counter);
 }
 
@@ -622,8 +659,6 @@ __global__ void __launch_bounds__(SC_THREADS) rows_fold_compute_kernel(const S* 
       acc2 += (rowf[1][f] - rowf[0][f]) * s2.get();
     }
   }
-  acc0 = block_sum(acc0);
-  acc2 = block_sum(acc2);
   finish_pairs(acc0, acc2, partials, out, counter);
 }
 
