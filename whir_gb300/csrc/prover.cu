@@ -46,6 +46,10 @@ int set_error(int code, const std::string& msg) {
 enum ProfFamily { PF_ENCODE = 0, PF_MERKLE, PF_SUMCHECK, PF_EQ, PF_GEOMETRIC, PF_LIFT, PF_POW, PF_GATHER,
                   PF_UNIVARIATE, PF_COUNT };
 
+static constexpr size_t MAIL_FLAG_OFF = 128;
+static constexpr size_t MAIL_DATA_OFF = 256;
+static constexpr size_t MAIL_DATA_BYTES = 512 * 1024;
+
 struct whir_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -57,9 +61,12 @@ struct whir_ctx {
   uint8_t* h_up = nullptr;  // pinned upload arena (see h2d)
   size_t up_cap = 0, up_off = 0;
   unsigned long long* d_pow = nullptr;
-  // Host-mapped pinned words the round kernels publish their (c0, c2) into (see wait_pair).
+  // Host-mapped pinned mail area: the round kernels publish their (c0, c2) at offset 0 (see
+  // SumcheckBuffers::wait_pair); small device results are copied to MAIL_DATA_OFF with a sequence
+  // word at MAIL_FLAG_OFF (see d2h2).
   uint8_t* mail_h = nullptr;
   uint8_t* mail_d = nullptr;
+  unsigned int mail_seq = 0;
   uint64_t launches_at_create = 0;
   uint64_t h2d_bytes = 0, d2h_bytes = 0;
   // profiling: event pairs recorded around each kernel family on the context's stream
@@ -166,16 +173,76 @@ void stage_reserve(whir_ctx* ctx, size_t bytes) {
   ctx->h_stage_cap = cap;
 }
 
-// Device -> host copy of a small result; waits for the stream.
-void d2h(whir_ctx* ctx, void* dst, const void* src, size_t bytes) {
-  if (!bytes) return;
-  ctx->d2h_bytes += bytes;
-  stage_reserve(ctx, bytes);
-  CU(cudaMemcpyAsync(ctx->h_stage, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
-  CU(cudaStreamSynchronize(ctx->stream));
-  ctx->up_off = 0;  // every earlier upload has completed
-  memcpy(dst, ctx->h_stage, bytes);
+}  // namespace
+
+// Copies up to two device segments into the context's host-mapped mail area and then publishes
+// `seq` in the mail flag word (after a system-wide fence), so the host can poll for the data
+// instead of synchronising the stream. One block; 16-, 8- or 1-byte moves by alignment.
+__global__ void __launch_bounds__(512) mail_copy_kernel(const uint8_t* s0, size_t b0, const uint8_t* s1, size_t b1,
+                                                         uint8_t* dst, size_t off1, unsigned int* flag,
+                                                         unsigned int seq) {
+  auto copy = [](const uint8_t* src, size_t bytes, uint8_t* d) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(d) | bytes;
+    if ((a & 15) == 0) {
+      for (size_t i = threadIdx.x; i < bytes / 16; i += blockDim.x)
+        reinterpret_cast<uint4*>(d)[i] = reinterpret_cast<const uint4*>(src)[i];
+    } else if ((a & 7) == 0) {
+      for (size_t i = threadIdx.x; i < bytes / 8; i += blockDim.x)
+        reinterpret_cast<uint64_t*>(d)[i] = reinterpret_cast<const uint64_t*>(src)[i];
+    } else {
+      for (size_t i = threadIdx.x; i < bytes; i += blockDim.x) d[i] = src[i];
+    }
+  };
+  copy(s0, b0, dst);
+  if (b1) copy(s1, b1, dst + off1);
+  __threadfence_system();
+  __syncthreads();
+  if (threadIdx.x == 0) *reinterpret_cast<volatile unsigned int*>(flag) = seq;
 }
+
+namespace {
+
+// Device -> host copy of small results (two segments at most); returns once the stream has
+// executed everything enqueued before it. Segments that fit the mail area go through
+// mail_copy_kernel and a bounded poll of the flag; larger ones through a pinned staging copy and
+// a stream synchronisation.
+void d2h2(whir_ctx* ctx, void* dst0, const void* src0, size_t b0, void* dst1, const void* src1, size_t b1) {
+  if (!b0 && !b1) return;
+  ctx->d2h_bytes += b0 + b1;
+  const size_t off1 = (b0 + 15) & ~(size_t)15;
+  if (off1 + b1 <= MAIL_DATA_BYTES) {
+    const unsigned int seq = ++ctx->mail_seq;
+    unsigned int* flag_h = reinterpret_cast<unsigned int*>(ctx->mail_h + MAIL_FLAG_OFF);
+    mail_copy_kernel<<<1, 512, 0, ctx->stream>>>(static_cast<const uint8_t*>(src0), b0,
+                                                 static_cast<const uint8_t*>(src1), b1, ctx->mail_d + MAIL_DATA_OFF,
+                                                 off1, reinterpret_cast<unsigned int*>(ctx->mail_d + MAIL_FLAG_OFF),
+                                                 seq);
+    CU(cudaGetLastError());
+    note_launch();
+    const auto t0 = std::chrono::steady_clock::now();
+    for (uint64_t spin = 0; __atomic_load_n(flag_h, __ATOMIC_ACQUIRE) != seq; ++spin) {
+      if ((spin & 1023) == 1023) {
+        cudaError_t e = cudaStreamQuery(ctx->stream);
+        if (e != cudaSuccess && e != cudaErrorNotReady) throw Error(WHIR_ERR_CUDA, cudaGetErrorString(e));
+        if (e == cudaSuccess && __atomic_load_n(flag_h, __ATOMIC_ACQUIRE) != seq)
+          throw Error(WHIR_ERR_INTERNAL, "device copy finished without publishing");
+        if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(60))
+          throw Error(WHIR_ERR_CUDA, "timed out waiting for a device result");
+      }
+    }
+    if (b0) memcpy(dst0, ctx->mail_h + MAIL_DATA_OFF, b0);
+    if (b1) memcpy(dst1, ctx->mail_h + MAIL_DATA_OFF + off1, b1);
+  } else {
+    stage_reserve(ctx, off1 + b1);
+    if (b0) CU(cudaMemcpyAsync(ctx->h_stage, src0, b0, cudaMemcpyDeviceToHost, ctx->stream));
+    if (b1) CU(cudaMemcpyAsync(ctx->h_stage + off1, src1, b1, cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    if (b0) memcpy(dst0, ctx->h_stage, b0);
+    if (b1) memcpy(dst1, ctx->h_stage + off1, b1);
+  }
+  ctx->up_off = 0;  // every earlier upload has completed
+}
+void d2h(whir_ctx* ctx, void* dst, const void* src, size_t bytes) { d2h2(ctx, dst, src, bytes, nullptr, nullptr, 0); }
 // Host -> device copy of a small argument (stream ordered; host buffer reusable on return).
 // Host -> device copy of a small argument without waiting: the bytes are staged in a pinned upload
 // arena whose space is recycled only after the stream has been synchronised (every d2h() does).
@@ -457,14 +524,7 @@ void irs_open(whir_ctx* ctx, const Irs& c, Transcript& ts, const std::vector<con
       CU(launch_gather_rows<F>(reinterpret_cast<const F*>(w->matrix.p), nc, d_idx.p, q, d_rows.p, ctx->stream));
       CU(launch_gather_digests(w->nodes.p, d_idx.p + q, nodes_idx.size(), d_sib.p, ctx->stream));
     }
-    stage_reserve(ctx, sub.size() * sizeof(F) + sib.size());
-    ctx->d2h_bytes += sub.size() * sizeof(F) + sib.size();
-    CU(cudaMemcpyAsync(ctx->h_stage, d_rows.p, sub.size() * sizeof(F), cudaMemcpyDeviceToHost, ctx->stream));
-    CU(cudaMemcpyAsync(ctx->h_stage + sub.size() * sizeof(F), d_sib.p, sib.size(), cudaMemcpyDeviceToHost,
-                       ctx->stream));
-    CU(cudaStreamSynchronize(ctx->stream));
-    memcpy(sub.data(), ctx->h_stage, sub.size() * sizeof(F));
-    memcpy(sib.data(), ctx->h_stage + sub.size() * sizeof(F), sib.size());
+    d2h2(ctx, sub.data(), d_rows.p, sub.size() * sizeof(F), sib.data(), d_sib.p, sib.size());
     // prover_hint_ark(&submatrix): ark-serialize compressed Vec<F> = u64 LE length + elements.
     uint8_t lb[8];
     uint64_t len = sub.size();
@@ -1093,8 +1153,8 @@ int whir_ctx_create(int device, whir_ctx** out) {
     CU(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
     root_tab<Gl>(ctx.get());  // the other fields' tables are built on first use
     CU(cudaMalloc((void**)&ctx->d_pow, 2 * sizeof(unsigned long long)));
-    CU(cudaHostAlloc((void**)&ctx->mail_h, 4096, cudaHostAllocMapped));
-    memset(ctx->mail_h, 0, 4096);
+    CU(cudaHostAlloc((void**)&ctx->mail_h, MAIL_DATA_OFF + MAIL_DATA_BYTES, cudaHostAllocMapped));
+    memset(ctx->mail_h, 0, MAIL_DATA_OFF + MAIL_DATA_BYTES);
     CU(cudaHostGetDevicePointer((void**)&ctx->mail_d, ctx->mail_h, 0));
     stage_reserve(ctx.get(), 1 << 20);
     ctx->up_cap = 8 << 20;
