@@ -13,6 +13,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/whir_gb300.h"
@@ -797,6 +798,46 @@ std::vector<T> eq_weights_host(const std::vector<T>& point) {
   return t;
 }
 
+// Host accumulator of 64x64-bit products: exact sum as lo (128 bits) + hi * 2^128, reduced mod p
+// once (2^128 = -2^32 mod p).
+struct HostAcc {
+  unsigned __int128 lo = 0;
+  uint64_t hi = 0;
+  void add(uint64_t a, uint64_t b) {
+    const unsigned __int128 p = (unsigned __int128)a * b;
+    lo += p;
+    hi += lo < p;
+  }
+  uint64_t reduce() const { return gl_sub(gl_reduce((uint64_t)lo, (uint64_t)(lo >> 64)), hi << 32); }
+};
+
+// sum_k w[k] * map(v[k]) for the opened rows of a STIR round, with unreduced products for the
+// Goldilocks family (the same field element as the reduced sum).
+template <class T, class S>
+T dot_host_wide(const T* w, const S* v, size_t n) {
+  if constexpr (std::is_same_v<S, Gl> && (std::is_same_v<T, Gl> || std::is_same_v<T, Gl2> || std::is_same_v<T, Gl3>)) {
+    HostAcc acc[T::DEG];
+    for (size_t k = 0; k < n; ++k)
+      for (int d = 0; d < T::DEG; ++d) acc[d].add(w[k].coeff(d).v, v[k].v);
+    uint64_t c[T::DEG];
+    for (int d = 0; d < T::DEG; ++d) c[d] = acc[d].reduce();
+    return Canon<T>::from(c);
+  } else if constexpr (std::is_same_v<T, Gl2> && std::is_same_v<S, Gl2>) {
+    HostAcc a00, a11, a01;
+    for (size_t k = 0; k < n; ++k) {
+      a00.add(w[k].c0, v[k].c0);
+      a11.add(w[k].c1, v[k].c1);
+      a01.add(w[k].c0, v[k].c1);
+      a01.add(w[k].c1, v[k].c0);
+    }
+    return Gl2{gl_add(a00.reduce(), gl_mul7(a11.reduce())), a01.reduce()};
+  } else {
+    T acc = T::zero();
+    for (size_t k = 0; k < n; ++k) acc += Embed<T, S>::mul(w[k], v[k]);
+    return acc;
+  }
+}
+
 template <class T>
 T dot_host(const std::vector<T>& a, const std::vector<T>& b) {
   T acc = T::zero();
@@ -946,14 +987,12 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
     std::unique_ptr<whir_witness> nw = irs_commit<T, T>(ctx, rc.irs, ts, a.p, cfg.field);
     pow_prove(ctx, rc.pow, ts);
     std::vector<typename T::Base> pts;
+    std::vector<S> srows;
     std::vector<T> in_rows;
     std::vector<uint64_t> exps;
     const size_t prev_N = prev ? cfg.rounds[ri - 1].irs.codeword_length : cfg.initial.codeword_length;
     if (!prev) {
-      std::vector<S> srows;
       irs_open<S>(ctx, cfg.initial, ts, witnesses, pts, srows, &exps);
-      in_rows.resize(srows.size());
-      for (size_t i = 0; i < srows.size(); ++i) in_rows[i] = Embed<T, S>::map(srows[i]);
     } else {
       irs_open<T>(ctx, cfg.rounds[ri - 1].irs, ts, std::vector<const whir_witness*>{prev.get()}, pts, in_rows,
                   &exps);
@@ -971,13 +1010,11 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
       std::vector<T> wts;
       for (const T& x : vector_rlc)
         for (const T& y : eqw) wts.push_back(x * y);
-      const size_t cols = pts.empty() ? 0 : in_rows.size() / pts.size();
+      const size_t cols = pts.empty() ? 0 : (prev ? in_rows.size() : srows.size()) / pts.size();
       if (cols != wts.size()) throw Error(WHIR_ERR_INTERNAL, "opened row width mismatch");
-      for (size_t pi = 0; pi < pts.size(); ++pi) {
-        T acc = T::zero();
-        for (size_t k = 0; k < cols; ++k) acc += wts[k] * in_rows[pi * cols + k];
-        stir_evals.push_back(acc);
-      }
+      for (size_t pi = 0; pi < pts.size(); ++pi)
+        stir_evals.push_back(prev ? dot_host_wide<T, T>(wts.data(), &in_rows[pi * cols], cols)
+                                  : dot_host_wide<T, S>(wts.data(), &srows[pi * cols], cols));
     }
     std::vector<T> stir_rlc = geometric_challenge<T>(ts, stir_points.size());
     if (nood) {
