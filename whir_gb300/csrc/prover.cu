@@ -10,6 +10,7 @@
 #include <chrono>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -68,6 +69,17 @@ struct whir_ctx {
   uint8_t* mail_h = nullptr;
   uint8_t* mail_d = nullptr;
   unsigned int mail_seq = 0;
+  // Sumcheck reduction scratch: per-block partial pairs and the (arrival, sequence) counter pair.
+  void* sc_parts = nullptr;
+  size_t sc_parts_bytes = 0;
+  unsigned int* sc_counter = nullptr;
+  unsigned int sc_launches = 0;
+  // Device buffers released by finished operations, kept for reuse by exact size. All of the
+  // context's work is issued on its one stream, so a buffer released in stream order can be handed
+  // to later work as the stream-ordered pool would, without an allocator call per buffer.
+  std::mutex cache_mu;
+  std::multimap<size_t, void*> free_bufs;
+  size_t cached_bytes = 0;
   uint64_t launches_at_create = 0;
   uint64_t h2d_bytes = 0, d2h_bytes = 0;
   // profiling: event pairs recorded around each kernel family on the context's stream
@@ -138,7 +150,38 @@ struct DeviceGuard {
   }
 };
 
-// Stream-ordered device buffer.
+// Per-context cache of released device buffers (exact-size reuse, bounded).
+static constexpr size_t BUF_CACHE_BYTES = 1ull << 30;        // bytes kept per context
+static constexpr size_t BUF_CACHE_MAX_BLOCK = 512ull << 20;  // larger buffers go back to the pool
+
+void* ctx_alloc(whir_ctx* ctx, size_t bytes) {
+  {
+    std::lock_guard<std::mutex> lk(ctx->cache_mu);
+    auto it = ctx->free_bufs.find(bytes);
+    if (it != ctx->free_bufs.end()) {
+      void* p = it->second;
+      ctx->free_bufs.erase(it);
+      ctx->cached_bytes -= bytes;
+      return p;
+    }
+  }
+  void* p = nullptr;
+  CU(cudaMallocAsync(&p, bytes, ctx->stream));
+  return p;
+}
+void ctx_release(whir_ctx* ctx, void* p, size_t bytes) {
+  {
+    std::lock_guard<std::mutex> lk(ctx->cache_mu);
+    if (bytes <= BUF_CACHE_MAX_BLOCK && ctx->cached_bytes + bytes <= BUF_CACHE_BYTES) {
+      ctx->free_bufs.emplace(bytes, p);
+      ctx->cached_bytes += bytes;
+      return;
+    }
+  }
+  cudaFreeAsync(p, ctx->stream);
+}
+
+// Stream-ordered device buffer (from the context's cache or the pool).
 template <class T>
 struct DBuf {
   whir_ctx* ctx = nullptr;
@@ -146,7 +189,7 @@ struct DBuf {
   size_t n = 0;
   DBuf() = default;
   DBuf(whir_ctx* c, size_t count) : ctx(c), n(count) {
-    if (count) CU(cudaMallocAsync((void**)&p, count * sizeof(T), c->stream));
+    if (count) p = static_cast<T*>(ctx_alloc(c, count * sizeof(T)));
   }
   DBuf(const DBuf&) = delete;
   DBuf& operator=(const DBuf&) = delete;
@@ -160,7 +203,7 @@ struct DBuf {
     return *this;
   }
   void release() {
-    if (p) cudaFreeAsync(p, ctx->stream);
+    if (p) ctx_release(ctx, p, n * sizeof(T));
     p = nullptr;
   }
   ~DBuf() { release(); }
@@ -396,8 +439,8 @@ uint64_t grind(whir_ctx* ctx, int kind, const uint8_t chal[32], uint64_t thresho
   while ((double)chunk < 64.0 * expect && chunk < (1ull << 36)) chunk <<= 1;
   const uint64_t limit = 1ull << 50;
   for (uint64_t start = 0; start < limit; start += chunk) {
-    CU(cudaMemsetAsync(ctx->d_pow, 0xff, sizeof(unsigned long long), ctx->stream));
-    CU(cudaMemsetAsync(ctx->d_pow + 1, 0, sizeof(unsigned long long), ctx->stream));
+    const unsigned long long init[2] = {~0ull, 0ull};  // best nonce, claimed-block counter
+    h2d(ctx, ctx->d_pow, init, sizeof(init));
     {
       ProfScope prof(ctx, PF_POW);
       CU(launch_pow(cw, threshold, start, chunk, ctx->d_pow, kind, ctx->stream));
@@ -548,16 +591,26 @@ void irs_open(whir_ctx* ctx, const Irs& c, Transcript& ts, const std::vector<con
 // sequence) and the output pair, which lives in the context's host-mapped mail words: the kernel's
 // last block writes (c0, c2) there and then the launch sequence, and the host polls that word
 // (wait_pair) instead of issuing a copy and synchronising the stream.
+// The partials area and the counter pair are the context's (allocated once; the counter is zeroed
+// at creation, the arrival count is re-armed by every last block and the launch sequence only grows,
+// mirrored on the host in ctx->sc_launches).
 template <class T>
 struct SumcheckBuffers {
   whir_ctx* ctx;
-  DBuf<T> parts;
-  DBuf<unsigned int> counter;
+  struct {
+    T* p;
+  } parts;
+  struct {
+    unsigned int* p;
+  } counter;
   T* out;    // device alias of the mail words
   T* out_h;  // host view
-  unsigned int launches = 0;
-  SumcheckBuffers(whir_ctx* c, size_t n) : ctx(c), parts(c, 2 * sumcheck_partials(n) + 2), counter(c, 2) {
-    CU(cudaMemsetAsync(counter.p, 0, 2 * sizeof(unsigned int), ctx->stream));
+  unsigned int& launches;
+  SumcheckBuffers(whir_ctx* c, size_t n) : ctx(c), launches(c->sc_launches) {
+    const size_t need = (2 * sumcheck_partials(n) + 2) * sizeof(T);
+    if (need > ctx->sc_parts_bytes) throw Error(WHIR_ERR_INTERNAL, "sumcheck partials area too small");
+    parts.p = reinterpret_cast<T*>(ctx->sc_parts);
+    counter.p = ctx->sc_counter;
     out = reinterpret_cast<T*>(ctx->mail_d);
     out_h = reinterpret_cast<T*>(ctx->mail_h);
   }
@@ -1190,6 +1243,10 @@ int whir_ctx_create(int device, whir_ctx** out) {
     CU(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
     root_tab<Gl>(ctx.get());  // the other fields' tables are built on first use
     CU(cudaMalloc((void**)&ctx->d_pow, 2 * sizeof(unsigned long long)));
+    ctx->sc_parts_bytes = (2 * sumcheck_partials(SIZE_MAX / 64) + 2) * 64;  // max blocks x largest element pair
+    CU(cudaMalloc(&ctx->sc_parts, ctx->sc_parts_bytes));
+    CU(cudaMalloc((void**)&ctx->sc_counter, 2 * sizeof(unsigned int)));
+    CU(cudaMemset(ctx->sc_counter, 0, 2 * sizeof(unsigned int)));
     CU(cudaHostAlloc((void**)&ctx->mail_h, MAIL_DATA_OFF + MAIL_DATA_BYTES, cudaHostAllocMapped));
     memset(ctx->mail_h, 0, MAIL_DATA_OFF + MAIL_DATA_BYTES);
     CU(cudaHostGetDevicePointer((void**)&ctx->mail_d, ctx->mail_h, 0));
@@ -1217,6 +1274,9 @@ int whir_ctx_destroy(whir_ctx* ctx) {
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
   if (ctx->h_up) cudaFreeHost(ctx->h_up);
   if (ctx->mail_h) cudaFreeHost(ctx->mail_h);
+  if (ctx->sc_parts) cudaFree(ctx->sc_parts);
+  for (auto& b : ctx->free_bufs) cudaFree(b.second);
+  if (ctx->sc_counter) cudaFree(ctx->sc_counter);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return 0;
