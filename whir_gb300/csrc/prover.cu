@@ -10,6 +10,7 @@
 #include <chrono>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -246,45 +247,69 @@ __global__ void __launch_bounds__(512) mail_copy_kernel(const uint8_t* s0, size_
 
 namespace {
 
-// Device -> host copy of small results (two segments at most); returns once the stream has
-// executed everything enqueued before it. Segments that fit the mail area go through
-// mail_copy_kernel and a bounded poll of the flag; larger ones through a pinned staging copy and
-// a stream synchronisation.
-void d2h2(whir_ctx* ctx, void* dst0, const void* src0, size_t b0, void* dst1, const void* src1, size_t b1) {
-  if (!b0 && !b1) return;
+// Device -> host copy of up to two segments, in two halves so that the host can enqueue more work
+// before waiting. Segments that fit the mail area go through mail_copy_kernel and a bounded poll of
+// its flag; larger ones are copied through pinned staging with a stream synchronisation at once.
+struct MailFetch {
+  void* dst0 = nullptr;
+  void* dst1 = nullptr;
+  size_t b0 = 0, b1 = 0, off1 = 0;
+  unsigned int seq = 0;
+  bool done = true;
+};
+MailFetch mail_begin(whir_ctx* ctx, void* dst0, const void* src0, size_t b0, void* dst1, const void* src1, size_t b1) {
+  MailFetch f;
+  f.dst0 = dst0;
+  f.dst1 = dst1;
+  f.b0 = b0;
+  f.b1 = b1;
+  f.off1 = (b0 + 15) & ~(size_t)15;
+  if (!b0 && !b1) return f;
   ctx->d2h_bytes += b0 + b1;
-  const size_t off1 = (b0 + 15) & ~(size_t)15;
-  if (off1 + b1 <= MAIL_DATA_BYTES) {
-    const unsigned int seq = ++ctx->mail_seq;
-    unsigned int* flag_h = reinterpret_cast<unsigned int*>(ctx->mail_h + MAIL_FLAG_OFF);
+  if (f.off1 + b1 <= MAIL_DATA_BYTES) {
+    f.seq = ++ctx->mail_seq;
+    f.done = false;
     mail_copy_kernel<<<1, 512, 0, ctx->stream>>>(static_cast<const uint8_t*>(src0), b0,
                                                  static_cast<const uint8_t*>(src1), b1, ctx->mail_d + MAIL_DATA_OFF,
-                                                 off1, reinterpret_cast<unsigned int*>(ctx->mail_d + MAIL_FLAG_OFF),
-                                                 seq);
+                                                 f.off1, reinterpret_cast<unsigned int*>(ctx->mail_d + MAIL_FLAG_OFF),
+                                                 f.seq);
     CU(cudaGetLastError());
     note_launch();
-    const auto t0 = std::chrono::steady_clock::now();
-    for (uint64_t spin = 0; __atomic_load_n(flag_h, __ATOMIC_ACQUIRE) != seq; ++spin) {
-      if ((spin & 1023) == 1023) {
-        cudaError_t e = cudaStreamQuery(ctx->stream);
-        if (e != cudaSuccess && e != cudaErrorNotReady) throw Error(WHIR_ERR_CUDA, cudaGetErrorString(e));
-        if (e == cudaSuccess && __atomic_load_n(flag_h, __ATOMIC_ACQUIRE) != seq)
-          throw Error(WHIR_ERR_INTERNAL, "device copy finished without publishing");
-        if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(60))
-          throw Error(WHIR_ERR_CUDA, "timed out waiting for a device result");
-      }
-    }
-    if (b0) memcpy(dst0, ctx->mail_h + MAIL_DATA_OFF, b0);
-    if (b1) memcpy(dst1, ctx->mail_h + MAIL_DATA_OFF + off1, b1);
   } else {
-    stage_reserve(ctx, off1 + b1);
+    stage_reserve(ctx, f.off1 + b1);
     if (b0) CU(cudaMemcpyAsync(ctx->h_stage, src0, b0, cudaMemcpyDeviceToHost, ctx->stream));
-    if (b1) CU(cudaMemcpyAsync(ctx->h_stage + off1, src1, b1, cudaMemcpyDeviceToHost, ctx->stream));
+    if (b1) CU(cudaMemcpyAsync(ctx->h_stage + f.off1, src1, b1, cudaMemcpyDeviceToHost, ctx->stream));
     CU(cudaStreamSynchronize(ctx->stream));
+    ctx->up_off = 0;  // every earlier upload has completed
     if (b0) memcpy(dst0, ctx->h_stage, b0);
-    if (b1) memcpy(dst1, ctx->h_stage + off1, b1);
+    if (b1) memcpy(dst1, ctx->h_stage + f.off1, b1);
   }
-  ctx->up_off = 0;  // every earlier upload has completed
+  return f;
+}
+// Waits (bounded) for a fetch started by mail_begin and copies its bytes out of the mail area.
+void mail_end(whir_ctx* ctx, MailFetch& f) {
+  if (f.done) return;
+  const unsigned int* flag_h = reinterpret_cast<const unsigned int*>(ctx->mail_h + MAIL_FLAG_OFF);
+  const auto t0 = std::chrono::steady_clock::now();
+  for (uint64_t spin = 0; __atomic_load_n(flag_h, __ATOMIC_ACQUIRE) != f.seq; ++spin) {
+    if ((spin & 1023) == 1023) {
+      cudaError_t e = cudaStreamQuery(ctx->stream);
+      if (e != cudaSuccess && e != cudaErrorNotReady) throw Error(WHIR_ERR_CUDA, cudaGetErrorString(e));
+      if (e == cudaSuccess && __atomic_load_n(flag_h, __ATOMIC_ACQUIRE) != f.seq)
+        throw Error(WHIR_ERR_INTERNAL, "device copy finished without publishing");
+      if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(60))
+        throw Error(WHIR_ERR_CUDA, "timed out waiting for a device result");
+    }
+  }
+  if (f.b0) memcpy(f.dst0, ctx->mail_h + MAIL_DATA_OFF, f.b0);
+  if (f.b1) memcpy(f.dst1, ctx->mail_h + MAIL_DATA_OFF + f.off1, f.b1);
+  f.done = true;
+}
+// Synchronous form: returns once the stream has executed everything enqueued before it.
+void d2h2(whir_ctx* ctx, void* dst0, const void* src0, size_t b0, void* dst1, const void* src1, size_t b1) {
+  MailFetch f = mail_begin(ctx, dst0, src0, b0, dst1, src1, b1);
+  mail_end(ctx, f);
+  ctx->up_off = 0;  // nothing was enqueued after the copy, so every earlier upload has completed
 }
 void d2h(whir_ctx* ctx, void* dst, const void* src, size_t bytes) { d2h2(ctx, dst, src, bytes, nullptr, nullptr, 0); }
 // Host -> device copy of a small argument (stream ordered; host buffer reusable on return).
@@ -534,11 +559,27 @@ std::unique_ptr<whir_witness> irs_commit(whir_ctx* ctx, const Irs& c, Transcript
   return w;
 }
 
-// irs_commit::Config::open (irs_commit.rs:385-432): returns evaluation points and the opened rows
-// (points x (witnesses * num_cols)) in the witnesses' field F.
+// irs_commit::Config::open (irs_commit.rs:385-432) in two halves. irs_open_begin samples the query
+// indices, computes the evaluation points (and their root exponents), launches the row and sibling
+// gathers of every witness and starts their copy to the host; irs_open_end waits for the copy,
+// writes the hints (Vec<F> submatrix, then the authentication nodes, per witness) and returns the
+// opened rows (points x (witnesses * num_cols)) in the witnesses' field F. Hints are not absorbed
+// by the sponge, so the caller may squeeze further challenges and enqueue more device work between
+// the two halves without changing the transcript.
 template <class F>
-void irs_open(whir_ctx* ctx, const Irs& c, Transcript& ts, const std::vector<const whir_witness*>& ws,
-              std::vector<typename F::Base>& points, std::vector<F>& rows, std::vector<uint64_t>* exps = nullptr) {
+struct OpenState {
+  size_t q = 0, nc = 0, nwit = 0, nodes = 0;
+  DBuf<uint64_t> d_idx;
+  DBuf<F> d_rows;        // nwit x q x nc
+  DBuf<uint32_t> d_sib;  // nwit x nodes x 8 words
+  std::vector<F> sub;
+  std::vector<uint8_t> sib;
+  MailFetch fetch;
+};
+
+template <class F>
+void irs_open_begin(whir_ctx* ctx, const Irs& c, Transcript& ts, const std::vector<const whir_witness*>& ws,
+                    std::vector<typename F::Base>& points, OpenState<F>& st, std::vector<uint64_t>* exps = nullptr) {
   std::vector<uint64_t> idx = challenge_indices(ts, c.codeword_length, c.in_domain_samples, c.dedup);
   points = evaluation_points<typename F::Base>(c.masked_message_length(), c.codeword_length, idx);
   if (exps) {
@@ -549,39 +590,60 @@ void irs_open(whir_ctx* ctx, const Irs& c, Transcript& ts, const std::vector<con
     exps->clear();
     for (uint64_t i : idx) exps->push_back(i / C + (i % C) * K);
   }
-  const size_t nc = c.num_cols, stride = ws.size() * nc, q = idx.size();
-  rows.assign(q * stride, F::zero());
+  st.nc = c.num_cols;
+  st.q = idx.size();
+  st.nwit = ws.size();
   std::vector<uint64_t> nodes_idx = merkle_open_nodes(c.layers, idx);
-  DBuf<uint64_t> d_idx(ctx, std::max<size_t>(q + nodes_idx.size(), 1));
+  st.nodes = nodes_idx.size();
+  st.d_idx = DBuf<uint64_t>(ctx, std::max<size_t>(st.q + st.nodes, 1));
   std::vector<uint64_t> both(idx);
   both.insert(both.end(), nodes_idx.begin(), nodes_idx.end());
-  h2d(ctx, d_idx.p, both.data(), both.size() * sizeof(uint64_t));
-  DBuf<F> d_rows(ctx, std::max<size_t>(q * nc, 1));
-  DBuf<uint32_t> d_sib(ctx, std::max<size_t>(nodes_idx.size() * 8, 1));
-  std::vector<F> sub(q * nc);
-  std::vector<uint8_t> sib(nodes_idx.size() * 32);
-  size_t off = 0;
-  for (const whir_witness* w : ws) {
-    if (w->codeword_len != c.codeword_length || w->num_cols != nc) throw Error(WHIR_ERR_INVALID, "witness shape mismatch");
-    {
-      ProfScope prof(ctx, PF_GATHER);
-      CU(launch_gather_rows<F>(reinterpret_cast<const F*>(w->matrix.p), nc, d_idx.p, q, d_rows.p, ctx->stream));
-      CU(launch_gather_digests(w->nodes.p, d_idx.p + q, nodes_idx.size(), d_sib.p, ctx->stream));
-    }
-    d2h2(ctx, sub.data(), d_rows.p, sub.size() * sizeof(F), sib.data(), d_sib.p, sib.size());
+  h2d(ctx, st.d_idx.p, both.data(), both.size() * sizeof(uint64_t));
+  const size_t per_rows = st.q * st.nc, per_sib = st.nodes * 8;
+  st.d_rows = DBuf<F>(ctx, std::max<size_t>(st.nwit * per_rows, 1));
+  st.d_sib = DBuf<uint32_t>(ctx, std::max<size_t>(st.nwit * per_sib, 1));
+  for (size_t k = 0; k < ws.size(); ++k) {
+    const whir_witness* w = ws[k];
+    if (w->codeword_len != c.codeword_length || w->num_cols != st.nc)
+      throw Error(WHIR_ERR_INVALID, "witness shape mismatch");
+    ProfScope prof(ctx, PF_GATHER);
+    CU(launch_gather_rows<F>(reinterpret_cast<const F*>(w->matrix.p), st.nc, st.d_idx.p, st.q,
+                             st.d_rows.p + k * per_rows, ctx->stream));
+    CU(launch_gather_digests(w->nodes.p, st.d_idx.p + st.q, st.nodes, st.d_sib.p + k * per_sib, ctx->stream));
+  }
+  st.sub.resize(st.nwit * per_rows);
+  st.sib.resize(st.nwit * st.nodes * 32);
+  st.fetch = mail_begin(ctx, st.sub.data(), st.d_rows.p, st.sub.size() * sizeof(F), st.sib.data(), st.d_sib.p,
+                        st.sib.size());
+}
+
+template <class F>
+void irs_open_end(whir_ctx* ctx, Transcript& ts, OpenState<F>& st, std::vector<F>& rows) {
+  mail_end(ctx, st.fetch);
+  const size_t nc = st.nc, q = st.q, stride = st.nwit * nc, per_rows = q * nc;
+  rows.assign(q * stride, F::zero());
+  for (size_t k = 0; k < st.nwit; ++k) {
+    const F* sub = st.sub.data() + k * per_rows;
     // prover_hint_ark(&submatrix): ark-serialize compressed Vec<F> = u64 LE length + elements.
     uint8_t lb[8];
-    uint64_t len = sub.size();
+    const uint64_t len = per_rows;
     for (int i = 0; i < 8; ++i) lb[i] = (uint8_t)(len >> (8 * i));
     ts.hint_bytes(lb, 8);
-    std::vector<uint8_t> eb(sub.size() * 8 * F::LIMBS);
-    for (size_t i = 0; i < sub.size(); ++i) elem_bytes(sub[i], eb.data() + i * 8 * F::LIMBS);
+    std::vector<uint8_t> eb(per_rows * 8 * F::LIMBS);
+    for (size_t i = 0; i < per_rows; ++i) elem_bytes(sub[i], eb.data() + i * 8 * F::LIMBS);
     ts.hint_bytes(eb.data(), eb.size());
-    ts.hint_bytes(sib.data(), sib.size());
+    ts.hint_bytes(st.sib.data() + k * st.nodes * 32, st.nodes * 32);
     for (size_t pi = 0; pi < q; ++pi)
-      for (size_t k = 0; k < nc; ++k) rows[pi * stride + off + k] = sub[pi * nc + k];
-    off += nc;
+      for (size_t j = 0; j < nc; ++j) rows[pi * stride + k * nc + j] = sub[pi * nc + j];
   }
+}
+
+template <class F>
+void irs_open(whir_ctx* ctx, const Irs& c, Transcript& ts, const std::vector<const whir_witness*>& ws,
+              std::vector<typename F::Base>& points, std::vector<F>& rows, std::vector<uint64_t>* exps = nullptr) {
+  OpenState<F> st;
+  irs_open_begin<F>(ctx, c, ts, ws, points, st, exps);
+  irs_open_end<F>(ctx, ts, st, rows);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -639,12 +701,19 @@ struct SumcheckBuffers {
   }
 };
 
+// `before_first_message` (optional) runs after the first round's kernel has been enqueued and
+// before its message is read: the caller finishes host work that the first round message needs
+// (the claimed sum) while the device computes.
 template <class T>
-std::vector<T> sumcheck_device(whir_ctx* ctx, const Sumcheck& c, Transcript& ts, T* a, T* b, size_t& n, T& sum) {
+std::vector<T> sumcheck_device(whir_ctx* ctx, const Sumcheck& c, Transcript& ts, T* a, T* b, size_t& n, T& sum,
+                               const std::function<void()>& before_first_message = {}) {
   if (c.mask_length != 0) throw Error(WHIR_ERR_UNSUPPORTED, "masked sumcheck is not part of this prover");
   if (n != c.initial_size) throw Error(WHIR_ERR_INTERNAL, "sumcheck size mismatch");
   std::vector<T> rs;
-  if (c.num_rounds == 0) return rs;
+  if (c.num_rounds == 0) {
+    if (before_first_message) before_first_message();
+    return rs;
+  }
   SumcheckBuffers<T> buf(ctx, n);
   bool have = false;
   T prev = T::zero();
@@ -660,6 +729,7 @@ std::vector<T> sumcheck_device(whir_ctx* ctx, const Sumcheck& c, Transcript& ts,
         n = n > 1 ? n / 2 : n;
       }
     }
+    if (round == 0 && before_first_message) before_first_message();
     T cc[2];
     buf.wait_pair(cc);
     const T c0 = cc[0], c2 = cc[1];
@@ -1044,11 +1114,15 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
     std::vector<T> in_rows;
     std::vector<uint64_t> exps;
     const size_t prev_N = prev ? cfg.rounds[ri - 1].irs.codeword_length : cfg.initial.codeword_length;
+    // The opening's rows come back while the device accumulates the STIR constraints and runs the
+    // first sumcheck round: the rows only feed the claimed sum (hints are not absorbed).
+    OpenState<S> open_s;
+    OpenState<T> open_t;
     if (!prev) {
-      irs_open<S>(ctx, cfg.initial, ts, witnesses, pts, srows, &exps);
+      irs_open_begin<S>(ctx, cfg.initial, ts, witnesses, pts, open_s, &exps);
     } else {
-      irs_open<T>(ctx, cfg.rounds[ri - 1].irs, ts, std::vector<const whir_witness*>{prev.get()}, pts, in_rows,
-                  &exps);
+      irs_open_begin<T>(ctx, cfg.rounds[ri - 1].irs, ts, std::vector<const whir_witness*>{prev.get()}, pts, open_t,
+                        &exps);
     }
     std::vector<T> stir_points;
     std::vector<T> stir_evals;
@@ -1058,17 +1132,6 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
       stir_evals.push_back(get_raw<T>(&nw->ood_matrix[o * T::LIMBS]));
     }
     for (const auto& p : pts) stir_points.push_back(T::from_base(p));
-    {
-      std::vector<T> eqw = eq_weights_host(folding);
-      std::vector<T> wts;
-      for (const T& x : vector_rlc)
-        for (const T& y : eqw) wts.push_back(x * y);
-      const size_t cols = pts.empty() ? 0 : (prev ? in_rows.size() : srows.size()) / pts.size();
-      if (cols != wts.size()) throw Error(WHIR_ERR_INTERNAL, "opened row width mismatch");
-      for (size_t pi = 0; pi < pts.size(); ++pi)
-        stir_evals.push_back(prev ? dot_host_wide<T, T>(wts.data(), &in_rows[pi * cols], cols)
-                                  : dot_host_wide<T, S>(wts.data(), &srows[pi * cols], cols));
-    }
     std::vector<T> stir_rlc = geometric_challenge<T>(ts, stir_points.size());
     if (nood) {
       // Out-of-domain points are general extension elements.
@@ -1080,8 +1143,24 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
       CU(launch_geometric_accumulate<T>(b.p, len, sp.p, sp.p + nood, nood, ctx->stream));
     }
     accumulate_in_domain<T>(ctx, b.p, len, std::vector<T>(stir_rlc.begin() + nood, stir_rlc.end()), exps, prev_N);
-    the_sum += dot_host(stir_rlc, stir_evals);
-    folding = sumcheck_device<T>(ctx, rc.sumcheck, ts, a.p, b.p, len, the_sum);
+    const std::vector<T> eqw = eq_weights_host(folding);
+    auto finish_open = [&]() {
+      if (!prev) {
+        irs_open_end<S>(ctx, ts, open_s, srows);
+      } else {
+        irs_open_end<T>(ctx, ts, open_t, in_rows);
+      }
+      std::vector<T> wts;
+      for (const T& x : vector_rlc)
+        for (const T& y : eqw) wts.push_back(x * y);
+      const size_t cols = pts.empty() ? 0 : (prev ? in_rows.size() : srows.size()) / pts.size();
+      if (cols != wts.size()) throw Error(WHIR_ERR_INTERNAL, "opened row width mismatch");
+      for (size_t pi = 0; pi < pts.size(); ++pi)
+        stir_evals.push_back(prev ? dot_host_wide<T, T>(wts.data(), &in_rows[pi * cols], cols)
+                                  : dot_host_wide<T, S>(wts.data(), &srows[pi * cols], cols));
+      the_sum += dot_host(stir_rlc, stir_evals);
+    };
+    folding = sumcheck_device<T>(ctx, rc.sumcheck, ts, a.p, b.p, len, the_sum, finish_open);
     evaluation_point.insert(evaluation_point.end(), folding.begin(), folding.end());
     prev = std::move(nw);
     vector_rlc = {T::one()};
