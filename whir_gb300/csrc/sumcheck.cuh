@@ -399,13 +399,30 @@ __global__ void __launch_bounds__(GR_THREADS) geometric_roots_kernel(T* acc, uin
       sStep[k] = root_pow<B>(rt, logN, (e * GR_THREADS) & mask);
     }
     __syncthreads();
-    for (int j = 0; j < cnt; ++j) {
-      T p = sS[j].mul_base(root_pow<B>(rt, logN, (sE[j] * i0) & mask));
-      const B step = sStep[j];
+    if constexpr (E == 1) {
+      // One index per thread: unreduced accumulation, with the root-table reads of 8 queries issued
+      // together (they are independent, and their latency dominates this loop).
+      WideAcc<T> w;
+      w.init();
+      int j = 0;
+      for (; j + 8 <= cnt; j += 8) {
+        B r[8];
 #pragma unroll
-      for (int u = 0; u < E; ++u) {
-        accu[u] += p;
-        if (u + 1 < E) p = p.mul_base(step);
+        for (int k = 0; k < 8; ++k) r[k] = root_pow<B>(rt, logN, (sE[j + k] * i0) & mask);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) w.mac_mixed(sS[j + k], r[k]);
+      }
+      for (; j < cnt; ++j) w.mac_mixed(sS[j], root_pow<B>(rt, logN, (sE[j] * i0) & mask));
+      accu[0] += w.get();
+    } else {
+      for (int j = 0; j < cnt; ++j) {
+        T p = sS[j].mul_base(root_pow<B>(rt, logN, (sE[j] * i0) & mask));
+        const B step = sStep[j];
+#pragma unroll
+        for (int u = 0; u < E; ++u) {
+          accu[u] += p;
+          if (u + 1 < E) p = p.mul_base(step);
+        }
       }
     }
   }
