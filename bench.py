@@ -35,9 +35,9 @@ FALLBACK_HBM_GBS = 6800.0
 
 # DRAM traffic / algorithmic bytes of a kernel family, from one ncu capture (profiles/
 # ncu_encode_and_first_sumcheck_d24.md): the initial commitment's encode_cols + encode_rows moved
-# 352.5 + 549.0 MB of DRAM for 402,653,184 algorithmic bytes. The encode kernels' traffic grows in
+# 350.1 + 549.8 MB of DRAM for 402,653,184 algorithmic bytes. The encode kernels' traffic grows in
 # proportion to the elements they process, so per-launch traffic = algorithmic bytes x this ratio.
-NCU_TRAFFIC_RATIO = {"encode": (352.507648e6 + 548.952832e6) / 402653184.0}
+NCU_TRAFFIC_RATIO = {"encode": (134.336e6 + 215.801088e6 + 268.765952e6 + 281.025024e6) / 402653184.0}
 
 
 def parse_args():
