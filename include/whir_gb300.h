@@ -131,6 +131,21 @@ int whir_prove(whir_ctx* ctx, const whir_config* cfg, whir_prover_state* ps, con
                size_t n_points, const uint64_t* covectors, size_t n_covectors, const uint64_t* evaluations,
                uint64_t* eval_point_out, uint64_t* rlc_out);
 
+/* Config::verify (src/protocols/whir/verifier.rs:45-265) followed by FinalClaim::verify
+ * (src/protocols/whir/mod.rs:63-74) against the statement, on the host (no device needed).
+ *   session:       the session string the prover state was created with
+ *   narg / hints:  the proof (whir_prover_state_proof)
+ *   n_commitments: number of witnesses the prover committed (each batch_size vectors)
+ *   mle_points, covectors, evaluations: the statement, laid out as for whir_prove
+ * Returns WHIR_OK when the proof is accepted, WHIR_REJECT when a check fails (the reason is in
+ * whir_verify_last_reason()), or a negative status for bad arguments. */
+int whir_verify(const whir_config* cfg, const char* session, size_t session_len, const uint8_t* narg,
+                size_t narg_len, const uint8_t* hints, size_t hints_len, size_t n_commitments,
+                const uint64_t* mle_points, size_t n_points, const uint64_t* covectors, size_t n_covectors,
+                const uint64_t* evaluations);
+/* Reason of the calling thread's last whir_verify rejection or error (no reference counterpart). */
+const char* whir_verify_last_reason(void);
+
 /* ---- operator-level entry points --------------------------------------------------------------- */
 /* ReedSolomon::interleaved_encode (src/algebra/ntt/mod.rs:89-99, cooley_tukey.rs:411-477) via
  * ntt::interleaved_rs_encode (ntt/mod.rs:120-128). msgs: n_msgs x msg_len (message-major); out:

@@ -70,6 +70,7 @@ def test_gpu_proof_equals_oracle_proof(ctx, orc, case):
     assert np.array_equal(claim.evaluation_point.reshape(-1), ref.evaluation_point)
     assert np.array_equal(claim.rlc_coefficients.reshape(-1), ref.rlc_coefficients)
     assert orc.whir_verify(f, op, nv, session, nw, narg, hints, pts, covs, evals)
+    assert W.Config(field, 1 << nv, params).verify(session, narg, hints, nw, pts, covs, evals)
 
 
 def test_gpu_proof_is_identical_across_runs_and_contexts(ctx, orc):
@@ -130,7 +131,10 @@ def test_d24_goldilocks2_verifies(ctx, orc):
     ev = orc.multilinear_extend(orc.GOLDILOCKS2, vec.reshape(-1), pt.reshape(-1))
     narg, hints, claim, roots = gpu_prove(ctx, "Goldilocks2", params, 24, "d24", vec, [pt], [], [[ev]], 1)
     assert orc.whir_verify(orc.GOLDILOCKS2, op, 24, "d24", 1, narg, hints, [pt], [], [[ev]])
+    cfg = W.Config("Goldilocks2", 1 << 24, params)
+    assert cfg.verify("d24", narg, hints, 1, [pt], [], [[ev]])
     bad = bytearray(hints)
     bad[100] ^= 4
     assert not orc.whir_verify(orc.GOLDILOCKS2, op, 24, "d24", 1, narg, bytes(bad), [pt], [], [[ev]])
+    assert not cfg.verify("d24", narg, bytes(bad), 1, [pt], [], [[ev]])
     assert hashlib.sha256(narg).hexdigest() != hashlib.sha256(hints).hexdigest()

@@ -90,6 +90,13 @@ def load_library():
     return _lib
 
 
+def last_verify_reason():
+    """Why the calling thread's last verification was rejected (or failed)."""
+    lib = load_library()
+    lib.whir_verify_last_reason.restype = ctypes.c_char_p
+    return lib.whir_verify_last_reason().decode()
+
+
 def _check(rc):
     if rc != 0:
         raise WhirError(rc, load_library().whir_last_error().decode())
@@ -326,6 +333,27 @@ class Config:
                               _u64ptr(cov) if cov is not None else None, ctypes.c_size_t(len(covectors)),
                               _u64ptr(ev) if ev is not None else None, _u64ptr(ep), _u64ptr(rl)))
         return FinalClaim(ep.reshape(nv, L) if L > 1 else ep, rl[: (len(points) + len(covectors)) * L])
+
+    def verify(self, session, narg, hints, n_commitments, points=(), covectors=(), evaluations=()):
+        """Config::verify + FinalClaim::verify on the host: True when the proof is accepted, False when
+        a check fails (reason in `last_verify_reason()`); raises WhirError on bad arguments."""
+        lib = load_library()
+        s = session.encode()
+        pts = _as_u64(np.asarray(points, dtype=np.uint64).reshape(-1)) if len(points) else None
+        cov = _as_u64(np.asarray(covectors, dtype=np.uint64).reshape(-1)) if len(covectors) else None
+        ev = _as_u64(np.asarray(evaluations, dtype=np.uint64).reshape(-1)) if len(evaluations) else None
+        nb = np.frombuffer(bytes(narg) or b"\0", dtype=np.uint8).copy()
+        hb = np.frombuffer(bytes(hints) or b"\0", dtype=np.uint8).copy()
+        rc = lib.whir_verify(self._h, s, ctypes.c_size_t(len(s)), _u8ptr(nb), ctypes.c_size_t(len(narg)), _u8ptr(hb),
+                             ctypes.c_size_t(len(hints)), ctypes.c_size_t(n_commitments),
+                             _u64ptr(pts) if pts is not None else None, ctypes.c_size_t(len(points)),
+                             _u64ptr(cov) if cov is not None else None, ctypes.c_size_t(len(covectors)),
+                             _u64ptr(ev) if ev is not None else None)
+        if rc == 1:
+            return False
+        if rc != 0:
+            raise WhirError(rc, last_verify_reason())
+        return True
 
     def __del__(self):
         try:

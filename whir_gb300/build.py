@@ -11,7 +11,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libwhir_gb300.so")
-SOURCES = ["commit.cu", "commit_mont.cu", "sumcheck.cu", "sumcheck_mont.cu", "prover.cu", "noalloc.cu"]
+SOURCES = ["commit.cu", "commit_mont.cu", "sumcheck.cu", "sumcheck_mont.cu", "prover.cu", "verifier.cu",
+           "noalloc.cu"]
 HEADERS = ["field.cuh", "hash.cuh", "kernels.hpp", "protocol.hpp", "status.hpp", "roots.cuh", "encode.cuh",
            "sumcheck.cuh", "sponge.cuh", "wide.cuh"]
 

@@ -170,12 +170,14 @@ inline F get_raw(const uint64_t* w) {
   memcpy(&x, w, sizeof(F));
   return x;
 }
-template <class F>
-inline F challenge(Transcript& t) {
+// The challenge helpers take any transcript with verifier_bytes / a `sponge` member: the prover's
+// Transcript and the verifier's VerifierTranscript (verifier.cu).
+template <class F, class Ts>
+inline F challenge(Ts& t) {
   return ChallengeCodec<F>::squeeze(t.sponge);
 }
-template <class F>
-inline std::vector<F> geometric_challenge(Transcript& t, size_t count) {
+template <class F, class Ts>
+inline std::vector<F> geometric_challenge(Ts& t, size_t count) {
   if (count == 0) return {};
   if (count == 1) return {F::one()};
   F x = challenge<F>(t);
@@ -185,7 +187,8 @@ inline std::vector<F> geometric_challenge(Transcript& t, size_t count) {
   return r;
 }
 // challenge_indices (src/protocols/challenge_indices.rs:6-50).
-inline std::vector<uint64_t> challenge_indices(Transcript& t, uint64_t num_leaves, size_t count, bool dedup) {
+template <class Ts>
+inline std::vector<uint64_t> challenge_indices(Ts& t, uint64_t num_leaves, size_t count, bool dedup) {
   if (count == 0) return {};
   if (num_leaves == 0 || (num_leaves & (num_leaves - 1))) throw Error(-1, "num_leaves must be a power of two");
   if (num_leaves == 1) return dedup ? std::vector<uint64_t>{0} : std::vector<uint64_t>(count, 0);
@@ -469,6 +472,17 @@ inline Config config_new(int field, size_t size, const Params& wp) {
 }
 
 // Canonical configuration bytes hashed into the protocol id (SHA3-512).
+inline std::vector<uint8_t> config_bytes(const Config& c);
+
+}  // namespace whir
+
+// Opaque handle of the C ABI: a derived WHIR configuration.
+struct whir_config {
+  whir::Config cfg;
+};
+
+namespace whir {
+
 inline std::vector<uint8_t> config_bytes(const Config& c) {
   std::vector<uint8_t> o;
   auto u64 = [&](uint64_t v) {

@@ -431,9 +431,6 @@ struct whir_witness {
   }
 };
 
-struct whir_config {
-  Config cfg;
-};
 
 struct whir_prover_state {
   Transcript ts;
