@@ -78,8 +78,7 @@ __device__ __forceinline__ void sts(F* s, int i, const F& x) {
 // so the threads of a warp read consecutive entries. The table is in shared memory, or (TWG) read
 // through L1 from the global copy.
 template <class B, bool TWG>
-__device__ __forceinline__ B level_tw(const B* tw, int log2h, int pos) {
-  const int i = (1 << (log2h - 1)) - 1 + pos;
+__device__ __forceinline__ B tw_at(const B* tw, int i) {
   if constexpr (TWG) {
     return ldg_elem(tw + i);
   } else {
@@ -100,6 +99,14 @@ __device__ __forceinline__ void dif_step(F* s, int logn, int logB, int nvec, int
   const int stride = 1 << logstride;
   const int items_log = logn - LOGR;  // work items per vector = n / R
   const int total = nvec << items_log;
+  const int kstep = stride * es;
+  // swz is linear over GF(2), and an element index is the sum of disjoint bit fields (vector, block,
+  // offset j < stride, k * stride, each scaled by the power-of-two strides vs / es), so
+  // swz(base + k * kstep) = swz(base) ^ swz(k * kstep): the R per-k terms are shared by every work
+  // item of the step, and an index costs one XOR.
+  int kswz[R];
+#pragma unroll
+  for (int k = 0; k < R; ++k) kswz[k] = swz<F>(k * kstep);
   for (int t = threadIdx.x; t < total; t += blockDim.x) {
     int v, it;
     if (vec_fastest) {
@@ -110,26 +117,27 @@ __device__ __forceinline__ void dif_step(F* s, int logn, int logB, int nvec, int
       it = t & ((1 << items_log) - 1);
     }
     const int blk = it >> logstride, j = it & (stride - 1);
-    const int base = v * vs + (((blk << logB) + j) * es);
-    const int kstep = stride * es;
+    const int sbase = swz<F>(v * vs + (((blk << logB) + j) * es));
     int pidx[R];
     F x[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-      pidx[k] = swz<F>(base + k * kstep);
+      pidx[k] = sbase ^ kswz[k];
       x[k] = lds(s, pidx[k]);
     }
 #pragma unroll
     for (int st = 0; st < LOGR; ++st) {
       const int half = R >> (st + 1);
       const int log2h = logB - st;
+      // w_(2h)^pos with pos = (j + k * stride) mod 2^log2h = j + (k mod 2^(LOGR - st)) * stride.
+      const int tw0 = (1 << (log2h - 1)) - 1 + j;
 #pragma unroll
       for (int k = 0; k < R; ++k) {
         if (k & half) continue;
-        const int pos = (j + k * stride) & ((1 << log2h) - 1);
+        const int kk = k & ((1 << (LOGR - st)) - 1);
         const F u = x[k], w = x[k + half];
         x[k] = u + w;
-        x[k + half] = (u - w).mul_base(level_tw<typename F::Base, TWG>(tw, log2h, pos));
+        x[k + half] = (u - w).mul_base(tw_at<typename F::Base, TWG>(tw, tw0 + kk * stride));
       }
     }
 #pragma unroll
