@@ -138,3 +138,28 @@ def test_d24_goldilocks2_verifies(ctx, orc):
     assert not orc.whir_verify(orc.GOLDILOCKS2, op, 24, "d24", 1, narg, bytes(bad), [pt], [], [[ev]])
     assert not cfg.verify("d24", narg, bytes(bad), 1, [pt], [], [[ev]])
     assert hashlib.sha256(narg).hexdigest() != hashlib.sha256(hints).hexdigest()
+
+
+@pytest.mark.parametrize("field,nv,bs,ud", [("Goldilocks2", 22, 1, True), ("Goldilocks3", 20, 7, False)])
+def test_staged_host_upload_matches_device_input(ctx, orc, field, nv, bs, ud):
+    # Host inputs of at least 16 MiB are copied in message groups on a second stream while the
+    # encode's first pass runs (32 MiB: 2 groups of 8 messages; 56 MiB: 3 uneven groups of 112
+    # messages). The proof equals the one made from a device-resident copy and the oracle's.
+    params = W.ProtocolParameters(unique_decoding=ud, security_level=100, pow_bits=16, batch_size=bs)
+    op = orc.make_params(unique_decoding=ud, security_level=100, pow_bits=16, batch_size=bs)
+    f, vecs, pts, covs, evals = statement(orc, field, nv, 1, bs, 1, False, seed=nv + bs)
+    narg_h, hints_h, _, _ = gpu_prove(ctx, field, params, nv, "staged", vecs, pts, covs, evals, 1)
+    flat = np.ascontiguousarray(vecs, dtype=np.uint64).reshape(-1)
+    dptr = ctx.alloc(flat.nbytes)
+    try:
+        ctx.upload(dptr, flat)
+        cfg = W.Config(field, 1 << nv, params)
+        ps = W.ProverState(cfg, "staged")
+        w = cfg.commit(ctx, ps, dptr, on_device=True)
+        cfg.prove(ctx, ps, dptr, [w], pts, covs, evals, on_device=True)
+        narg_d, hints_d = ps.proof()
+    finally:
+        ctx.free(dptr)
+    assert narg_h == narg_d and hints_h == hints_d
+    ref = orc.whir_prove(f, op, nv, "staged", vecs, pts, covs, evals)
+    assert narg_h == ref.narg and hints_h == ref.hints

@@ -428,9 +428,20 @@ static cudaError_t dispatch_rows(const EncArgs<F>& a, int kind, unsigned grid, s
 
 template <class F>
 cudaError_t launch_encode(const EncodePlan& p, const F* src, size_t n_msgs, size_t msg_len, F* dst,
-                          uint32_t* leaves, int hash_kind, F* scratch, RootTab rt, cudaStream_t s) {
+                          uint32_t* leaves, int hash_kind, F* scratch, RootTab rt, cudaStream_t s,
+                          const EncodeStaging* staging) {
   // Every root index below is taken modulo the codeword length, which must divide 2^log_order.
   if (p.logN > rt.log_order || p.logN > 32) return cudaErrorInvalidValue;
+  const int groups = staging ? staging->groups : 1;
+  if (groups < 1 || (size_t)groups > n_msgs) return cudaErrorInvalidValue;
+  if (staging) {
+    if (staging->bounds[0] != 0 || staging->bounds[groups] != n_msgs) return cudaErrorInvalidValue;
+    for (int g = 0; g < groups; ++g)
+      if (staging->bounds[g] >= staging->bounds[g + 1]) return cudaErrorInvalidValue;
+  }
+  auto wait_group = [&](int g) -> cudaError_t {
+    return staging ? cudaStreamWaitEvent(s, staging->ready[g], 0) : cudaSuccess;
+  };
   EncArgs<F> a;
   a.leaves = leaves;
   a.msg_len = msg_len;
@@ -444,6 +455,10 @@ cudaError_t launch_encode(const EncodePlan& p, const F* src, size_t n_msgs, size
   a.W = p.cols_per_cta;
   a.rt = rt;
   if (p.mode == 0) {
+    for (int g = 0; g < groups; ++g) {
+      cudaError_t e = wait_group(g);
+      if (e != cudaSuccess) return e;
+    }
     a.mode = 0;
     a.src = src;
     a.dst = dst;
@@ -451,23 +466,29 @@ cudaError_t launch_encode(const EncodePlan& p, const F* src, size_t n_msgs, size
     const size_t smem = (size_t)a.G * n_msgs * n * sizeof(F) + n * sizeof(typename F::Base) + 16;
     return dispatch_rows<F>(a, hash_kind, (unsigned)(a.K / a.G), smem, s);
   }
-  // pass 1
+  // pass 1, one launch per message group (messages are independent in this pass; a group's
+  // intermediate rows start at message m0's block [m0][c = 0][k1 = 0][j2 = 0])
   {
     static std::once_flag flags[ENC_MAX_DEVICES];
     static cudaError_t results[ENC_MAX_DEVICES];
     cudaError_t ea = smem_attr_once(encode_cols_kernel<F>, flags, results);
     if (ea != cudaSuccess) return ea;
-    EncArgs<F> c = a;
-    c.src = src;
-    c.dst = scratch;
-    c.leaves = nullptr;
     const size_t C1 = 1ull << p.logC1, C2 = 1ull << p.logC2;
     const size_t smem = (size_t)a.W * C1 * sizeof(F) + 16;
-    const size_t grid = n_msgs * a.K * (C2 / a.W);
-    encode_cols_kernel<F><<<(unsigned)grid, ENC_THREADS, smem, s>>>(c);
-    note_launch();
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    for (int g = 0; g < groups; ++g) {
+      cudaError_t e = wait_group(g);
+      if (e != cudaSuccess) return e;
+      const size_t m0 = staging ? staging->bounds[g] : 0, m1 = staging ? staging->bounds[g + 1] : n_msgs;
+      EncArgs<F> c = a;
+      c.src = src + m0 * msg_len;
+      c.dst = scratch + m0 * a.K * C1 * C2;
+      c.leaves = nullptr;
+      const size_t grid = (m1 - m0) * a.K * (C2 / a.W);
+      encode_cols_kernel<F><<<(unsigned)grid, ENC_THREADS, smem, s>>>(c);
+      note_launch();
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
   }
   // pass 2
   a.mode = 1;
@@ -532,7 +553,7 @@ cudaError_t launch_to_canonical(F* v, size_t n, cudaStream_t s) {
 
 #define WHIR_ENCODE_INST(F)                                                                                      \
   template cudaError_t launch_encode<F>(const EncodePlan&, const F*, size_t, size_t, F*, uint32_t*, int, F*, RootTab, \
-                                        cudaStream_t);                                                           \
+                                        cudaStream_t, const EncodeStaging*);                                     \
   template cudaError_t launch_gather_rows<F>(const F*, size_t, const uint64_t*, size_t, F*, cudaStream_t);       \
   template cudaError_t launch_to_internal<F>(F*, size_t, cudaStream_t);                                         \
   template cudaError_t launch_to_canonical<F>(F*, size_t, cudaStream_t);

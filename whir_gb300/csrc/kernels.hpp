@@ -48,12 +48,24 @@ struct EncodePlan {
 // Returns 0, or a negative status when the shape is unsupported on the device.
 int plan_encode(size_t n_msgs, size_t msg_len, size_t codeword_len, size_t elem_bytes, EncodePlan* plan);
 
+// Messages made resident by work on another stream, in `groups` consecutive message groups:
+// group g holds messages [bounds[g], bounds[g + 1]) (bounds[0] = 0, bounds[groups] = n_msgs), and
+// ready[g] is recorded once they are in place. The encode waits for each group's event just before
+// the first kernel that reads it, so the column passes of earlier groups overlap the copies of
+// later ones.
+struct EncodeStaging {
+  int groups;
+  const size_t* bounds;
+  const cudaEvent_t* ready;
+};
+
 // Encodes messages (n_msgs x msg_len, message-major) into dst (codeword_len x n_msgs, row-major).
 // When leaves != nullptr, also writes the digest of every row (canonical LE bytes of its elements)
 // with engine `hash_kind`. scratch must hold plan.scratch_elems elements.
 template <class F>
 cudaError_t launch_encode(const EncodePlan& plan, const F* src, size_t n_msgs, size_t msg_len, F* dst,
-                          uint32_t* leaves, int hash_kind, F* scratch, RootTab rt, cudaStream_t s);
+                          uint32_t* leaves, int hash_kind, F* scratch, RootTab rt, cudaStream_t s,
+                          const EncodeStaging* staging = nullptr);
 
 // Builds Merkle layers above the leaf layer in place. nodes: (2^(layers+1) - 1) digests laid out
 // [leaves (2^layers)][layer 1]...[root] (merkle_tree.rs:96-121).

@@ -56,6 +56,9 @@ static constexpr size_t MAIL_DATA_BYTES = 512 * 1024;
 struct whir_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  // Second stream for host-to-device copies of commit inputs that overlap the encode (see
+  // encode_and_tree); everything else runs on `stream`.
+  cudaStream_t up_stream = nullptr;
   // Root tables per base field (Goldilocks, Field192, Field256): lo (2^16) then hi entries.
   uint64_t* d_roots[3] = {nullptr, nullptr, nullptr};
   RootTab rts[3] = {};
@@ -488,9 +491,21 @@ void pow_prove(whir_ctx* ctx, const Pow& p, Transcript& ts) {
 // ------------------------------------------------------------------------------------------------
 // Interleaved RS commitment on the device (irs_commit.rs:292-350)
 // ------------------------------------------------------------------------------------------------
+// Inputs of at least this many bytes are uploaded in message groups that overlap the encode.
+static constexpr size_t STAGED_UPLOAD_MIN_BYTES = 16u << 20;
+static constexpr int STAGED_UPLOAD_MAX_GROUPS = 4;
+
+// Canonical host messages to copy into the encode's input buffer while the encode runs (the
+// Goldilocks family, whose in-memory form is the canonical one).
+template <class F>
+struct HostUpload {
+  const F* host;
+  F* dev;
+};
+
 template <class F>
 void encode_and_tree(whir_ctx* ctx, const F* d_msgs, size_t n_msgs, size_t msg_len, size_t codeword_len, int kind,
-                     whir_witness& w) {
+                     whir_witness& w, const HostUpload<F>* upload = nullptr) {
   EncodePlan plan;
   int rc = plan_encode(n_msgs, msg_len, codeword_len, sizeof(F), &plan);
   if (rc) throw Error(rc, "encode shape unsupported on the device");
@@ -504,11 +519,42 @@ void encode_and_tree(whir_ctx* ctx, const F* d_msgs, size_t n_msgs, size_t msg_l
   w.matrix = DBuf<uint64_t>(ctx, codeword_len * n_msgs * F::LIMBS);
   w.nodes = DBuf<uint32_t>(ctx, ((2ull << w.layers) - 1) * 8);
   DBuf<F> scratch(ctx, plan.scratch_elems);
+  // Staged upload: message groups are copied on the upload stream (after the work already queued on
+  // the context's stream, which may still use the reused input buffer), each followed by an event
+  // that the encode waits for before its first kernel reading that group.
+  std::vector<cudaEvent_t> ready;
+  std::vector<size_t> bounds;
+  EncodeStaging staging{1, nullptr, nullptr};
+  if (upload) {
+    const size_t bytes = n_msgs * msg_len * sizeof(F);
+    // Equal groups: smaller first groups (less of the copy exposed) measured slower overall, as the
+    // narrower column-pass launches leave more of their last wave idle.
+    const size_t ngroups = std::max<size_t>(
+        1, std::min<size_t>({n_msgs, (size_t)STAGED_UPLOAD_MAX_GROUPS, bytes / STAGED_UPLOAD_MIN_BYTES}));
+    for (size_t g = 0; g <= ngroups; ++g) bounds.push_back(n_msgs * g / ngroups);
+    const int groups = (int)bounds.size() - 1;
+    cudaEvent_t start = take_event(ctx);
+    ready.push_back(start);
+    CU(cudaEventRecord(start, ctx->stream));
+    CU(cudaStreamWaitEvent(ctx->up_stream, start, 0));
+    for (int g = 0; g < groups; ++g) {
+      const size_t m0 = bounds[g], m1 = bounds[g + 1];
+      CU(cudaMemcpyAsync(upload->dev + m0 * msg_len, upload->host + m0 * msg_len, (m1 - m0) * msg_len * sizeof(F),
+                         cudaMemcpyHostToDevice, ctx->up_stream));
+      cudaEvent_t e = take_event(ctx);
+      ready.push_back(e);
+      CU(cudaEventRecord(e, ctx->up_stream));
+    }
+    ctx->h2d_bytes += bytes;
+    staging = EncodeStaging{groups, bounds.data(), ready.data() + 1};
+  }
   {
     ProfScope prof(ctx, PF_ENCODE);
     CU(launch_encode<F>(plan, d_msgs, n_msgs, msg_len, reinterpret_cast<F*>(w.matrix.p), w.nodes.p, kind, scratch.p,
-                        root_tab<typename F::Base>(ctx), ctx->stream));
+                        root_tab<typename F::Base>(ctx), ctx->stream, upload ? &staging : nullptr));
   }
+  // A wait captures the event's state when it is enqueued, so the events can be reused at once.
+  for (cudaEvent_t e : ready) ctx->event_pool.push_back(e);
   {
     ProfScope prof(ctx, PF_MERKLE);
     CU(launch_merkle(w.nodes.p, (int)w.layers, kind, ctx->stream));
@@ -532,15 +578,24 @@ T univariate_device(whir_ctx* ctx, const S* d_coeffs, size_t n, const T& x) {
 }
 
 // vectors: num_vectors contiguous device vectors of S.
+// upload (optional): d_vecs is still to be filled from these host vectors; the copy overlaps the encode.
 template <class S, class T>
-std::unique_ptr<whir_witness> irs_commit(whir_ctx* ctx, const Irs& c, Transcript& ts, const S* d_vecs, int field) {
+std::unique_ptr<whir_witness> irs_commit(whir_ctx* ctx, const Irs& c, Transcript& ts, const S* d_vecs, int field,
+                                         const HostUpload<S>* upload = nullptr) {
   auto w = std::make_unique<whir_witness>();
   w->ctx = ctx;
   w->field = field;
   int kind = hash_kind_or_throw(c.hash_id);
   // Messages: each vector split into interleaving_depth contiguous chunks (irs_commit.rs:317-320),
   // so the contiguous vector array already is the n_msgs x message_length message matrix.
-  encode_and_tree<S>(ctx, d_vecs, c.num_cols, c.message_length(), c.codeword_length, kind, *w);
+  if (upload && c.num_cols * c.message_length() != c.num_vectors * c.vector_size) {
+    // the message matrix does not tile the vectors exactly: copy everything before encoding
+    CU(cudaMemcpyAsync(upload->dev, upload->host, c.num_vectors * c.vector_size * sizeof(S), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    ctx->h2d_bytes += c.num_vectors * c.vector_size * sizeof(S);
+    upload = nullptr;
+  }
+  encode_and_tree<S>(ctx, d_vecs, c.num_cols, c.message_length(), c.codeword_length, kind, *w, upload);
   ts.prover_bytes(w->root, 32);
   for (size_t i = 0; i < c.out_domain_samples; ++i) {
     put_raw(w->ood_points, challenge<T>(ts));
@@ -1312,6 +1367,7 @@ int whir_ctx_create(int device, whir_ctx** out) {
     ctx->device = device;
     CU(cudaSetDevice(device));
     CU(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    CU(cudaStreamCreateWithFlags(&ctx->up_stream, cudaStreamNonBlocking));
     // Keep freed pool memory cached across proofs.
     cudaMemPool_t pool;
     CU(cudaDeviceGetDefaultMemPool(&pool, device));
@@ -1339,6 +1395,7 @@ int whir_ctx_destroy(whir_ctx* ctx) {
   if (!ctx) return 0;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  if (ctx->up_stream) cudaStreamSynchronize(ctx->up_stream);
   for (auto& p : ctx->pending) {
     cudaEventDestroy(p.second.first);
     cudaEventDestroy(p.second.second);
@@ -1354,6 +1411,7 @@ int whir_ctx_destroy(whir_ctx* ctx) {
   for (auto& b : ctx->free_bufs) cudaFree(b.second);
   if (ctx->sc_counter) cudaFree(ctx->sc_counter);
   cudaStreamDestroy(ctx->stream);
+  if (ctx->up_stream) cudaStreamDestroy(ctx->up_stream);
   delete ctx;
   return 0;
 }
@@ -1543,8 +1601,16 @@ int whir_commit(whir_ctx* ctx, const whir_config* cfg, whir_prover_state* ps, co
     return with_embedding(c.field, [&]<class S, class T>() {
       const size_t count = c.initial.num_vectors * c.size();
       DBuf<S> copy;
-      const S* d = device_vectors<S>(ctx, vectors, count, flags, copy, false);
-      auto w = irs_commit<S, T>(ctx, c.initial, ps->ts, d, c.field);
+      std::unique_ptr<whir_witness> w;
+      if (!(flags & WHIR_DEVICE_PTRS) && Canon<S>::IDENTITY && count * sizeof(S) >= STAGED_UPLOAD_MIN_BYTES) {
+        // Large host input: the upload runs in message groups beside the encode's first pass.
+        copy = DBuf<S>(ctx, count);
+        const HostUpload<S> up{reinterpret_cast<const S*>(vectors), copy.p};
+        w = irs_commit<S, T>(ctx, c.initial, ps->ts, copy.p, c.field, &up);
+      } else {
+        const S* d = device_vectors<S>(ctx, vectors, count, flags, copy, false);
+        w = irs_commit<S, T>(ctx, c.initial, ps->ts, d, c.field);
+      }
       CU(cudaStreamSynchronize(ctx->stream));
       if (!(flags & WHIR_DEVICE_PTRS)) {
         // Keep the device copy: prove() given the same host buffer reuses it instead of copying again.
