@@ -136,6 +136,16 @@ def test_pow_lowest_nonce_parity(ctx, orc, engine, bits):
     assert W.pow_grind(ctx, engine, chal, thr) == orc.pow_grind(W.ENGINES[engine], chal, thr)
 
 
+@pytest.mark.parametrize("seed", range(6))
+def test_pow_blake3_split_round_parity(ctx, orc, seed):
+    # The Blake3 search computes the nonce-independent part of round 1 once per challenge; lowest
+    # nonces over several challenges and difficulties equal the oracle's full compressions.
+    chal = hashlib.sha256(b"split-%d" % seed).digest()
+    for bits in (3, 12, 18):
+        thr = orc.pow_threshold(float(bits))
+        assert W.pow_grind(ctx, "Blake3", chal, thr) == orc.pow_grind(W.ENGINES["Blake3"], chal, thr)
+
+
 def test_evaluation_points_parity(orc):
     for masked, cw in ((1, 2), (16, 64), (1 << 16, 1 << 20), (4, 1 << 16)):
         idx = np.array([0, 1, cw // 3, cw - 1], np.uint64)

@@ -184,6 +184,7 @@ cudaError_t launch_hash_many(const uint8_t* in, size_t size, size_t count, uint8
 // ---------------------------------------------------------------------------------------------
 struct PowArgs {
   uint32_t chal[8];
+  uint32_t pre[16];  // Blake3: state after the nonce-independent part of round 1 (blake3_pow_prefix)
   uint64_t threshold, start, count;
   unsigned long long* best;
   unsigned long long* counter;
@@ -211,20 +212,32 @@ __global__ void __launch_bounds__(POW_THREADS) pow_kernel(PowArgs a) {
     const unsigned long long st = s_start;
     __syncthreads();
     if (st == ~0ull) return;
+    // The best nonce so far is re-read before every hash (the read of one iteration is used by the
+    // next, so its latency hides behind a hash): once a satisfying nonce at or below this thread's
+    // next nonce is known, the rest of the block cannot lower the result and is skipped. Without
+    // this, every block claimed before the first hit ran to completion (about one full wave of
+    // nonces beyond the answer).
+    unsigned long long known = *reinterpret_cast<volatile unsigned long long*>(a.best);
 #pragma unroll 1
     for (int q = 0; q < POW_PER_THREAD; ++q) {
       const uint64_t off = (uint64_t)q * POW_THREADS + threadIdx.x;
       if (st - a.start + off >= a.count) break;
       const uint64_t nonce = st + off;
-      uint32_t m[16];
-#pragma unroll
-      for (int w = 0; w < 8; ++w) m[w] = a.chal[w];
-      m[8] = (uint32_t)nonce;
-      m[9] = (uint32_t)(nonce >> 32);
-#pragma unroll
-      for (int w = 10; w < 16; ++w) m[w] = 0;
+      if (nonce >= known) break;
+      known = *reinterpret_cast<volatile unsigned long long*>(a.best);
       uint32_t h[8];
-      hash64<KIND>(m, h);
+      if constexpr (KIND == HASH_BLAKE3) {
+        blake3_pow_tail(a.pre, a.chal, (uint32_t)nonce, (uint32_t)(nonce >> 32), h[0], h[1]);
+      } else {
+        uint32_t m[16];
+#pragma unroll
+        for (int w = 0; w < 8; ++w) m[w] = a.chal[w];
+        m[8] = (uint32_t)nonce;
+        m[9] = (uint32_t)(nonce >> 32);
+#pragma unroll
+        for (int w = 10; w < 16; ++w) m[w] = 0;
+        hash64<KIND>(m, h);
+      }
       const uint64_t v = (uint64_t)h[0] | ((uint64_t)h[1] << 32);
       if (v <= a.threshold) atomicMin(a.best, (unsigned long long)nonce);
     }
@@ -235,6 +248,7 @@ cudaError_t launch_pow(const uint32_t challenge[8], uint64_t threshold, uint64_t
                        unsigned long long* best, int kind, cudaStream_t s) {
   PowArgs a;
   for (int i = 0; i < 8; ++i) a.chal[i] = challenge[i];
+  blake3_pow_prefix(a.chal, a.pre);
   a.threshold = threshold;
   a.start = start;
   a.count = count;

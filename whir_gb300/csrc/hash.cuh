@@ -103,6 +103,43 @@ WHIR_HD void blake3_64(const uint32_t m[16], uint32_t out[8]) {
   blake3_compress_cv(out, m, 0, 0, 64, B3_CHUNK_START | B3_CHUNK_END | B3_ROOT);
 }
 
+// Proof-of-work blocks (proof_of_work.rs:81-104): m[0..8) = challenge, m[8..10) = nonce (LE),
+// m[10..16) = 0, hashed as blake3_64. Round 1 reads the nonce only in its first diagonal G; the
+// column step and the other three diagonal G's (disjoint state words, so their order is free) are
+// the same for every nonce of a search and are computed once by blake3_pow_prefix. blake3_pow_tail
+// finishes one nonce from that state and returns the first two output words.
+WHIR_HD void blake3_pow_prefix(const uint32_t c[8], uint32_t pre[16]) {
+  uint32_t s0 = Blake3IV::w(0), s1 = Blake3IV::w(1), s2 = Blake3IV::w(2), s3 = Blake3IV::w(3);
+  uint32_t s4 = Blake3IV::w(4), s5 = Blake3IV::w(5), s6 = Blake3IV::w(6), s7 = Blake3IV::w(7);
+  uint32_t s8 = Blake3IV::w(0), s9 = Blake3IV::w(1), s10 = Blake3IV::w(2), s11 = Blake3IV::w(3);
+  uint32_t s12 = 0, s13 = 0, s14 = 64, s15 = B3_CHUNK_START | B3_CHUNK_END | B3_ROOT;
+  WHIR_B3_G(s0, s4, s8, s12, c[0], c[1]);
+  WHIR_B3_G(s1, s5, s9, s13, c[2], c[3]);
+  WHIR_B3_G(s2, s6, s10, s14, c[4], c[5]);
+  WHIR_B3_G(s3, s7, s11, s15, c[6], c[7]);
+  WHIR_B3_G(s1, s6, s11, s12, 0u, 0u);
+  WHIR_B3_G(s2, s7, s8, s13, 0u, 0u);
+  WHIR_B3_G(s3, s4, s9, s14, 0u, 0u);
+  const uint32_t v[16] = {s0, s1, s2, s3, s4, s5, s6, s7, s8, s9, s10, s11, s12, s13, s14, s15};
+  for (int i = 0; i < 16; ++i) pre[i] = v[i];
+}
+WHIR_HD void blake3_pow_tail(const uint32_t pre[16], const uint32_t c[8], uint32_t n0, uint32_t n1, uint32_t& h0,
+                             uint32_t& h1) {
+  uint32_t s0 = pre[0], s1 = pre[1], s2 = pre[2], s3 = pre[3], s4 = pre[4], s5 = pre[5], s6 = pre[6], s7 = pre[7];
+  uint32_t s8 = pre[8], s9 = pre[9], s10 = pre[10], s11 = pre[11], s12 = pre[12], s13 = pre[13], s14 = pre[14],
+           s15 = pre[15];
+  WHIR_B3_G(s0, s5, s10, s15, n0, n1);
+  const uint32_t m[16] = {c[0], c[1], c[2], c[3], c[4], c[5], c[6], c[7], n0, n1, 0u, 0u, 0u, 0u, 0u, 0u};
+  WHIR_B3_ROUND(m[2], m[6], m[3], m[10], m[7], m[0], m[4], m[13], m[1], m[11], m[12], m[5], m[9], m[14], m[15], m[8]);
+  WHIR_B3_ROUND(m[3], m[4], m[10], m[12], m[13], m[2], m[7], m[14], m[6], m[5], m[9], m[0], m[11], m[15], m[8], m[1]);
+  WHIR_B3_ROUND(m[10], m[7], m[12], m[9], m[14], m[3], m[13], m[15], m[4], m[0], m[11], m[2], m[5], m[8], m[1], m[6]);
+  WHIR_B3_ROUND(m[12], m[13], m[9], m[11], m[15], m[10], m[14], m[8], m[7], m[2], m[5], m[3], m[0], m[1], m[6], m[4]);
+  WHIR_B3_ROUND(m[9], m[14], m[11], m[5], m[8], m[12], m[15], m[1], m[13], m[3], m[0], m[10], m[2], m[6], m[4], m[7]);
+  WHIR_B3_ROUND(m[11], m[15], m[5], m[0], m[1], m[9], m[8], m[6], m[14], m[10], m[2], m[12], m[3], m[4], m[7], m[13]);
+  h0 = s0 ^ s8;
+  h1 = s1 ^ s9;
+}
+
 // ------------------------------------------------------------------------------------------------
 // Keccak-f[1600]
 // ------------------------------------------------------------------------------------------------
