@@ -539,10 +539,12 @@ inline std::vector<uint8_t> config_bytes(const Config& c) {
 inline std::vector<uint64_t> merkle_open_nodes(size_t layers, std::vector<uint64_t> idx) {
   std::sort(idx.begin(), idx.end());
   idx.erase(std::unique(idx.begin(), idx.end()), idx.end());
-  std::vector<uint64_t> out;
+  std::vector<uint64_t> out, next;
+  out.reserve(idx.size() * layers);
+  next.reserve(idx.size());
   uint64_t off = 0, len = 1ull << layers;
   while (len > 1) {
-    std::vector<uint64_t> next;
+    next.clear();
     for (size_t i = 0; i < idx.size(); ++i) {
       uint64_t a = idx[i];
       if (i + 1 < idx.size() && idx[i + 1] == (a ^ 1)) {

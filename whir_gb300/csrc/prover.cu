@@ -154,8 +154,10 @@ struct DeviceGuard {
   }
 };
 
-// Per-context cache of released device buffers (exact-size reuse, bounded).
-static constexpr size_t BUF_CACHE_BYTES = 1ull << 30;        // bytes kept per context
+// Per-context cache of released device buffers (exact-size reuse, bounded). The bound holds every
+// buffer of a d = 24 proof (about 2 GiB), so repeated proofs of one shape allocate nothing: a
+// stream-ordered allocation that has to map new pool memory stalls the host for ~150 us.
+static constexpr size_t BUF_CACHE_BYTES = 4ull << 30;        // bytes kept per context
 static constexpr size_t BUF_CACHE_MAX_BLOCK = 512ull << 20;  // larger buffers go back to the pool
 
 void* ctx_alloc(whir_ctx* ctx, size_t bytes) {
@@ -631,9 +633,11 @@ struct OpenState {
 
 template <class F>
 void irs_open_begin(whir_ctx* ctx, const Irs& c, Transcript& ts, const std::vector<const whir_witness*>& ws,
-                    std::vector<typename F::Base>& points, OpenState<F>& st, std::vector<uint64_t>* exps = nullptr) {
+                    size_t& npoints, OpenState<F>& st, std::vector<uint64_t>* exps = nullptr) {
   std::vector<uint64_t> idx = challenge_indices(ts, c.codeword_length, c.in_domain_samples, c.dedup);
-  points = evaluation_points<typename F::Base>(c.masked_message_length(), c.codeword_length, idx);
+  // The prover needs only the number of evaluation points (their values enter the device's STIR
+  // accumulation as root exponents), so they are not computed on the host.
+  npoints = idx.size();
   if (exps) {
     // point = w_N^e with e = transpose_permute(index, K, C) (cooley_tukey.rs:391-399)
     uint64_t C = 1;
@@ -692,9 +696,9 @@ void irs_open_end(whir_ctx* ctx, Transcript& ts, OpenState<F>& st, std::vector<F
 
 template <class F>
 void irs_open(whir_ctx* ctx, const Irs& c, Transcript& ts, const std::vector<const whir_witness*>& ws,
-              std::vector<typename F::Base>& points, std::vector<F>& rows, std::vector<uint64_t>* exps = nullptr) {
+              size_t& npoints, std::vector<F>& rows, std::vector<uint64_t>* exps = nullptr) {
   OpenState<F> st;
-  irs_open_begin<F>(ctx, c, ts, ws, points, st, exps);
+  irs_open_begin<F>(ctx, c, ts, ws, npoints, st, exps);
   irs_open_end<F>(ctx, ts, st, rows);
 }
 
@@ -1161,7 +1165,7 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
     if (len != rc.irs.vector_size) throw Error(WHIR_ERR_INTERNAL, "round vector size mismatch");
     std::unique_ptr<whir_witness> nw = irs_commit<T, T>(ctx, rc.irs, ts, a.p, cfg.field);
     pow_prove(ctx, rc.pow, ts);
-    std::vector<typename T::Base> pts;
+    size_t npts = 0;
     std::vector<S> srows;
     std::vector<T> in_rows;
     std::vector<uint64_t> exps;
@@ -1171,11 +1175,13 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
     OpenState<S> open_s;
     OpenState<T> open_t;
     if (!prev) {
-      irs_open_begin<S>(ctx, cfg.initial, ts, witnesses, pts, open_s, &exps);
+      irs_open_begin<S>(ctx, cfg.initial, ts, witnesses, npts, open_s, &exps);
     } else {
-      irs_open_begin<T>(ctx, cfg.rounds[ri - 1].irs, ts, std::vector<const whir_witness*>{prev.get()}, pts, open_t,
+      irs_open_begin<T>(ctx, cfg.rounds[ri - 1].irs, ts, std::vector<const whir_witness*>{prev.get()}, npts, open_t,
                         &exps);
     }
+    // STIR constraint points: the commitment's out-of-domain points, then the opened in-domain
+    // points (only their count is needed here).
     std::vector<T> stir_points;
     std::vector<T> stir_evals;
     const size_t nood = nw->ood_points.size() / T::LIMBS;
@@ -1183,8 +1189,7 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
       stir_points.push_back(get_raw<T>(&nw->ood_points[o * T::LIMBS]));
       stir_evals.push_back(get_raw<T>(&nw->ood_matrix[o * T::LIMBS]));
     }
-    for (const auto& p : pts) stir_points.push_back(T::from_base(p));
-    std::vector<T> stir_rlc = geometric_challenge<T>(ts, stir_points.size());
+    std::vector<T> stir_rlc = geometric_challenge<T>(ts, nood + npts);
     if (nood) {
       // Out-of-domain points are general extension elements.
       DBuf<T> sp(ctx, 2 * nood);
@@ -1205,9 +1210,9 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
       std::vector<T> wts;
       for (const T& x : vector_rlc)
         for (const T& y : eqw) wts.push_back(x * y);
-      const size_t cols = pts.empty() ? 0 : (prev ? in_rows.size() : srows.size()) / pts.size();
+      const size_t cols = npts == 0 ? 0 : (prev ? in_rows.size() : srows.size()) / npts;
       if (cols != wts.size()) throw Error(WHIR_ERR_INTERNAL, "opened row width mismatch");
-      for (size_t pi = 0; pi < pts.size(); ++pi)
+      for (size_t pi = 0; pi < npts; ++pi)
         stir_evals.push_back(prev ? dot_host_wide<T, T>(wts.data(), &in_rows[pi * cols], cols)
                                   : dot_host_wide<T, S>(wts.data(), &srows[pi * cols], cols));
       the_sum += dot_host(stir_rlc, stir_evals);
@@ -1224,13 +1229,13 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
   for (const T& x : fin) send_elem<T>(ts, x);
   pow_prove(ctx, cfg.final_pow, ts);
   {
-    std::vector<typename T::Base> pts;
+    size_t npts = 0;
     if (!prev) {
       std::vector<S> rows;
-      irs_open<S>(ctx, cfg.initial, ts, witnesses, pts, rows);
+      irs_open<S>(ctx, cfg.initial, ts, witnesses, npts, rows);
     } else {
       std::vector<T> rows;
-      irs_open<T>(ctx, cfg.rounds.back().irs, ts, std::vector<const whir_witness*>{prev.get()}, pts, rows);
+      irs_open<T>(ctx, cfg.rounds.back().irs, ts, std::vector<const whir_witness*>{prev.get()}, npts, rows);
     }
   }
   std::vector<T> last = sumcheck_device<T>(ctx, cfg.final_sumcheck, ts, a.p, b.p, len, the_sum);
