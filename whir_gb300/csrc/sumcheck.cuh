@@ -502,6 +502,7 @@ cudaError_t launch_eq_table(const T* point, int off, int cnt, T scalar, T* table
 // by the row factor (linearity), so no per-row block reduction is needed.
 static constexpr uint64_t EQ_CHUNK = 2048;
 static constexpr int EQ_MAX_FORMS = 16;
+static constexpr int EQ_UNROLL = (int)(EQ_CHUNK / SC_THREADS);  // chunk elements per thread
 
 template <class T, class S>
 __global__ void __launch_bounds__(SC_THREADS) first_compute_eq_kernel(const S* x, uint64_t n, const T* tables,
@@ -627,7 +628,7 @@ __global__ void __launch_bounds__(SC_THREADS) first_fold_compute_eq_kernel(const
 // fstride) into F_next (per-form stride 2^h), and computes (c0, c2) of the next round from
 // row sums of lo-weighted a values. Needs rlog >= 2 and nforms <= EQ_MAX_FORMS.
 template <class T, class S>
-__global__ void __launch_bounds__(SC_THREADS) rows_fold_compute_kernel(const S* a_in, uint64_t m, T r, const T* F,
+__global__ void __launch_bounds__(SC_THREADS, sizeof(T) <= 16 ? 2 : 1) rows_fold_compute_kernel(const S* a_in, uint64_t m, T r, const T* F,
                                                                       uint64_t fstride, int rlog, const T* tables,
                                                                       int nforms, int h, int l, T* a_out,
                                                                       T* F_next, T* partials, T* out,
@@ -655,22 +656,53 @@ __global__ void __launch_bounds__(SC_THREADS) rows_fold_compute_kernel(const S* 
       WideAcc<T> s0, s2;
       s0.init();
       s2.init();
-      for (uint64_t j = j0 + threadIdx.x; j < j0 + chunk; j += blockDim.x) {
-        const uint64_t i = base + j;
-        T fa0, fa1;
-        if (f == 0) {
-          const S x0 = a_in[i], x1 = a_in[i + q], x2 = a_in[i + hf], x3 = a_in[i + hf + q];
-          fa0 = Embed<T, S>::map(x0) + Embed<T, S>::mul(r, x2 - x0);
-          fa1 = Embed<T, S>::map(x1) + Embed<T, S>::mul(r, x3 - x1);
-          a_out[i] = fa0;
-          a_out[i + q] = fa1;
-        } else {
-          fa0 = a_out[i];  // written by this thread in the first pass
-          fa1 = a_out[i + q];
+      if (f == 0 && chunk == EQ_CHUNK && sizeof(T) <= 16) {
+        // Full chunk of the first form: the fold's loads are issued in groups of RF_GROUP
+        // iterations before any of their stores. a_out may alias a_in, but a thread's stores
+        // (offsets i, i + q) never meet another iteration's loads (i', i' + q, i' + hf, i' + hf + q
+        // with i' != i inside one chunk, q >= chunk), so hoisting the loads is safe.
+        constexpr int RF_GROUP = sizeof(S) <= 8 ? 4 : 2;
+#pragma unroll 1
+        for (int k0 = 0; k0 < EQ_UNROLL; k0 += RF_GROUP) {
+          S x0[RF_GROUP], x1[RF_GROUP], x2[RF_GROUP], x3[RF_GROUP];
+#pragma unroll
+          for (int k = 0; k < RF_GROUP; ++k) {
+            const uint64_t i = base + j0 + threadIdx.x + (uint64_t)(k0 + k) * SC_THREADS;
+            x0[k] = a_in[i];
+            x1[k] = a_in[i + q];
+            x2[k] = a_in[i + hf];
+            x3[k] = a_in[i + hf + q];
+          }
+#pragma unroll
+          for (int k = 0; k < RF_GROUP; ++k) {
+            const uint64_t j = j0 + threadIdx.x + (uint64_t)(k0 + k) * SC_THREADS, i = base + j;
+            const T fa0 = Embed<T, S>::map(x0[k]) + Embed<T, S>::mul(r, x2[k] - x0[k]);
+            const T fa1 = Embed<T, S>::map(x1[k]) + Embed<T, S>::mul(r, x3[k] - x1[k]);
+            a_out[i] = fa0;
+            a_out[i + q] = fa1;
+            const T w = lo[j];
+            s0.mac(w, fa0);
+            s2.mac(w, fa1 - fa0);
+          }
         }
-        const T w = lo[j];
-        s0.mac(w, fa0);
-        s2.mac(w, fa1 - fa0);
+      } else {
+        for (uint64_t j = j0 + threadIdx.x; j < j0 + chunk; j += blockDim.x) {
+          const uint64_t i = base + j;
+          T fa0, fa1;
+          if (f == 0) {
+            const S x0 = a_in[i], x1 = a_in[i + q], x2 = a_in[i + hf], x3 = a_in[i + hf + q];
+            fa0 = Embed<T, S>::map(x0) + Embed<T, S>::mul(r, x2 - x0);
+            fa1 = Embed<T, S>::map(x1) + Embed<T, S>::mul(r, x3 - x1);
+            a_out[i] = fa0;
+            a_out[i + q] = fa1;
+          } else {
+            fa0 = a_out[i];  // written by this thread in the first pass
+            fa1 = a_out[i + q];
+          }
+          const T w = lo[j];
+          s0.mac(w, fa0);
+          s2.mac(w, fa1 - fa0);
+        }
       }
       acc0 += rowf[0][f] * s0.get();
       acc2 += (rowf[1][f] - rowf[0][f]) * s2.get();
