@@ -149,7 +149,8 @@ const char* whir_verify_last_reason(void);
 /* ---- operator-level entry points --------------------------------------------------------------- */
 /* ReedSolomon::interleaved_encode (src/algebra/ntt/mod.rs:89-99, cooley_tukey.rs:411-477) via
  * ntt::interleaved_rs_encode (ntt/mod.rs:120-128). msgs: n_msgs x msg_len (message-major); out:
- * codeword_len x n_msgs (row-major). Masks must be empty (mask_len == 0). */
+ * codeword_len x n_msgs (row-major). masks: n_msgs x mask_len (may be NULL when mask_len == 0);
+ * message m is encoded as its msg_len coefficients followed by its mask_len mask values. */
 int whir_rs_interleaved_encode(whir_ctx* ctx, int field, const uint64_t* msgs, size_t n_msgs, size_t msg_len,
                                const uint64_t* masks, size_t mask_len, size_t codeword_len, uint64_t* out,
                                uint32_t flags);

@@ -33,6 +33,38 @@ def test_encode_parity(ctx, orc, fname, fid, n_msgs, msg_len, codeword_len):
     assert np.array_equal(got, exp)
 
 
+@pytest.mark.parametrize("fname,fid", FIELDS)
+@pytest.mark.parametrize("n_msgs,msg_len,mask_len,codeword_len", [
+    (1, 1, 1, 4), (4, 6, 2, 16), (16, 1000, 24, 1 << 12), (3, 0, 5, 8), (16, 1 << 12, 3, 1 << 14),
+])
+def test_encode_with_masks_parity(ctx, orc, fname, fid, n_msgs, msg_len, mask_len, codeword_len):
+    # ReedSolomon::interleaved_encode with masks: message m is msgs[m] followed by masks[m], so the
+    # coset size follows msg_len + mask_len.
+    rng = Rng(n_msgs * 7 + msg_len * 3 + mask_len)
+    L = W.TARGET_LIMBS[fid]
+    msgs = field_elements(fname, n_msgs * msg_len, rng=rng).reshape(n_msgs, msg_len, L)
+    masks = field_elements(fname, n_msgs * mask_len, rng=rng).reshape(n_msgs, mask_len, L)
+    if L == 1:
+        msgs, masks = msgs.reshape(n_msgs, msg_len), masks.reshape(n_msgs, mask_len)
+    got = W.interleaved_encode(ctx, fid, msgs, codeword_len, masks=masks)
+    exp = orc.interleaved_encode(fid, msgs, masks, codeword_len)
+    assert np.array_equal(got, exp)
+
+
+def test_encode_rejects_unsupported_and_invalid_shapes(ctx):
+    # Non-power-of-two codewords (valid for the reference's mixed-radix engine, unused by WHIR) are
+    # refused with WHIR_ERR_UNSUPPORTED; a message longer than the codeword with WHIR_ERR_INVALID.
+    msgs = np.ones((2, 4), np.uint64)
+    with pytest.raises(W.WhirError) as e:
+        W.interleaved_encode(ctx, W.GOLDILOCKS1, msgs, 12)
+    assert e.value.code == -2
+    with pytest.raises(W.WhirError) as e:
+        W.interleaved_encode(ctx, W.GOLDILOCKS1, np.ones((2, 40), np.uint64), 32)
+    assert e.value.code == -1
+    with pytest.raises(W.WhirError):
+        W.interleaved_encode(ctx, W.GOLDILOCKS1, msgs, 16, masks=np.ones((3, 2), np.uint64))
+
+
 @pytest.mark.parametrize("fname,fid", FIELDS[3:])
 def test_encode_montgomery_fields_four_step(ctx, orc, fname, fid):
     # Field192/Field256 rows are 24/32 bytes per element: the d=20, rate-1/4 initial shape (16 messages

@@ -367,15 +367,21 @@ class Config:
 # ----------------------------------------------------------------------------------------------
 # Operator-level functions (host numpy in, host numpy out)
 # ----------------------------------------------------------------------------------------------
-def interleaved_encode(ctx, field, msgs, codeword_len):
-    """ntt::interleaved_rs_encode: msgs (n_msgs, msg_len[, limbs]) -> (codeword_len, n_msgs[, limbs])."""
+def interleaved_encode(ctx, field, msgs, codeword_len, masks=None):
+    """ntt::interleaved_rs_encode: msgs (n_msgs, msg_len[, limbs]) and optional masks (n_msgs, mask_len[, limbs])
+    -> (codeword_len, n_msgs[, limbs]); message m is encoded as msgs[m] followed by masks[m]."""
     L = TARGET_LIMBS[field]
     m = _as_u64(msgs)
     n_msgs, msg_len = m.shape[0], m.shape[1]
+    mk = _as_u64(masks) if masks is not None else None
+    mask_len = mk.shape[1] if mk is not None else 0
+    if mk is not None and mk.shape[0] != n_msgs:
+        raise WhirError(-1, "masks must have one row per message")
     out = np.zeros(codeword_len * n_msgs * L, dtype=np.uint64)
     _check(load_library().whir_rs_interleaved_encode(ctx._h, ctypes.c_int(field), _u64ptr(m), ctypes.c_size_t(n_msgs),
-                                                     ctypes.c_size_t(msg_len), None, ctypes.c_size_t(0),
-                                                     ctypes.c_size_t(codeword_len), _u64ptr(out), ctypes.c_uint32(0)))
+                                                     ctypes.c_size_t(msg_len), _u64ptr(mk) if mask_len else None,
+                                                     ctypes.c_size_t(mask_len), ctypes.c_size_t(codeword_len),
+                                                     _u64ptr(out), ctypes.c_uint32(0)))
     return out.reshape(codeword_len, n_msgs, L) if L > 1 else out.reshape(codeword_len, n_msgs)
 
 

@@ -1690,18 +1690,31 @@ int whir_rs_interleaved_encode(whir_ctx* ctx, int field, const uint64_t* msgs, s
                                uint32_t flags) {
   return guarded([&] {
     check_ctx(ctx);
-    (void)masks;
-    if (mask_len != 0) throw Error(WHIR_ERR_UNSUPPORTED, "masked encoding (ZK) is not part of this library");
+    if (mask_len != 0 && !masks) throw Error(WHIR_ERR_INVALID, "null masks with mask_len > 0");
     if (n_msgs == 0) return 0;
     return with_field(field, [&]<class F>() {
-      DBuf<F> in, outb;
+      DBuf<F> in, mk, cat, outb;
       const F* d_in = device_vectors<F>(ctx, msgs, n_msgs * msg_len, flags, in);
+      // Masked messages (cooley_tukey.rs:411-477): message m's coefficients are its msg_len values
+      // followed by its mask_len mask values (masks laid out [n_msgs][mask_len]); the rows are
+      // assembled on the device and encoded as messages of msg_len + mask_len coefficients.
+      const size_t len = msg_len + mask_len;
+      if (mask_len) {
+        const F* d_mk = device_vectors<F>(ctx, masks, n_msgs * mask_len, flags, mk);
+        cat = DBuf<F>(ctx, n_msgs * len);
+        if (msg_len)
+          CU(cudaMemcpy2DAsync(cat.p, len * sizeof(F), d_in, msg_len * sizeof(F), msg_len * sizeof(F), n_msgs,
+                               cudaMemcpyDeviceToDevice, ctx->stream));
+        CU(cudaMemcpy2DAsync(cat.p + msg_len, len * sizeof(F), d_mk, mask_len * sizeof(F), mask_len * sizeof(F),
+                             n_msgs, cudaMemcpyDeviceToDevice, ctx->stream));
+        d_in = cat.p;
+      }
       F* d_out = (flags & WHIR_DEVICE_PTRS) ? reinterpret_cast<F*>(out) : (outb = DBuf<F>(ctx, codeword_len * n_msgs)).p;
       EncodePlan plan;
-      int rc = plan_encode(n_msgs, msg_len, codeword_len, sizeof(F), &plan);
+      int rc = plan_encode(n_msgs, len, codeword_len, sizeof(F), &plan);
       if (rc) throw Error(rc, "encode shape unsupported on the device");
       DBuf<F> scratch(ctx, plan.scratch_elems);
-      CU(launch_encode<F>(plan, d_in, n_msgs, msg_len, d_out, nullptr, HASH_BLAKE3, scratch.p,
+      CU(launch_encode<F>(plan, d_in, n_msgs, len, d_out, nullptr, HASH_BLAKE3, scratch.p,
                           root_tab<typename F::Base>(ctx), ctx->stream));
       CU(launch_to_canonical<F>(d_out, codeword_len * n_msgs, ctx->stream));
       if (!(flags & WHIR_DEVICE_PTRS))
