@@ -34,10 +34,10 @@ MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 
 # DRAM traffic / algorithmic bytes of a kernel family, from one ncu capture (profiles/
-# ncu_encode_and_first_sumcheck_d24.md): the initial commitment's encode_cols + encode_rows moved
-# 350.1 + 549.8 MB of DRAM for 402,653,184 algorithmic bytes. The encode kernels' traffic grows in
-# proportion to the elements they process, so per-launch traffic = algorithmic bytes x this ratio.
-NCU_TRAFFIC_RATIO = {"encode": (134.336e6 + 215.801088e6 + 268.765952e6 + 281.025024e6) / 402653184.0}
+# ncu_encode_kernels_prove_d24_goldilocks2.md): the initial commitment's encode_cols + encode_rows
+# moved 350.8 + 549.7 MB of DRAM for 402,653,184 algorithmic bytes. The encode kernels' traffic grows
+# in proportion to the elements they process, so per-launch traffic = algorithmic bytes x this ratio.
+NCU_TRAFFIC_RATIO = {"encode": (134.601472e6 + 216.216576e6 + 268.512768e6 + 281.217536e6) / 402653184.0}
 
 
 def parse_args():
