@@ -88,7 +88,7 @@ def prove_job(ctx, job):
 
 
 class BatchProver:
-    def __init__(self, device=0, workers=4):
+    def __init__(self, device=0, workers=8):
         self.contexts = [Context(device) for _ in range(workers)]
 
     def prove_all(self, jobs):
@@ -129,7 +129,7 @@ class BatchProver:
 class ProofServer:
     """Continuous batching over `workers` contexts with admission by an HBM budget (bytes)."""
 
-    def __init__(self, device=0, workers=4, hbm_budget=150 << 30):
+    def __init__(self, device=0, workers=8, hbm_budget=150 << 30):
         self.contexts = [Context(device) for _ in range(workers)]
         self.budget = hbm_budget
 
