@@ -2,6 +2,7 @@
 // given stream and returns a cudaError_t (or a negative WHIR status for unsupported shapes); none
 // of them synchronizes.
 #pragma once
+#include <algorithm>
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -124,9 +125,39 @@ cudaError_t launch_geometric_accumulate(T* acc, size_t n, const T* scalars, cons
 
 // acc[i] += sum_j scalars[j] * w_N^(exps[j] * i) for i < n, points given as exponents of the
 // N-th root of unity (in-domain evaluation points). Device arrays; N = 2^logN.
+// Up to 4096 entries the (entry, query) pairs are also split over the queries: inside a CTA over
+// 2^te_log entries, and across `groups` CTAs per tile of entries (the late rounds' covectors:
+// 24 -> 5-9 us). Larger covectors keep one CTA thread per entry over all queries, where the
+// root-table gathers are bound by L2 sector traffic either way. With groups > 1 the CTAs
+// write partial sums (partials: groups * n elements) and the last CTA of a tile adds them (counters:
+// GR_MAX_TILES words, zero before the first launch, re-armed by the kernel). Without scratch the
+// launch uses one group.
+static constexpr int GR_MAX_TILES = 4096;
+struct GeometricSplit {
+  bool split;  // false: one entry per thread (or several) over all queries
+  int te_log;  // entries per CTA = 2^te_log (CTA threads / 2^te_log query subgroups)
+  int groups;  // query groups across CTAs per tile of entries
+};
+inline GeometricSplit geometric_split_plan(size_t n, size_t m, bool scratch) {
+  GeometricSplit p{false, 8, 1};
+  if (n == 0 || m == 0 || n > 4096) return p;
+  p.split = true;
+  int te = 0;
+  while (te < 8 && ((size_t)1 << te) < n) ++te;
+  p.te_log = te;
+  const size_t tiles = (n + ((size_t)1 << te) - 1) >> te, sub = (size_t)256 >> te;
+  if (scratch && tiles <= (size_t)GR_MAX_TILES) {
+    // about four waves of CTAs, at least eight queries per (CTA, subgroup)
+    size_t g = (608 + tiles - 1) / tiles;
+    g = std::min(g, std::max<size_t>(1, m / (8 * sub)));
+    p.groups = (int)std::max<size_t>(1, std::min<size_t>(g, 64));
+  }
+  return p;
+}
 template <class T>
 cudaError_t launch_geometric_roots(T* acc, size_t n, const T* scalars, const uint64_t* exps, size_t m, int logN,
-                                   RootTab rt, cudaStream_t s);
+                                   RootTab rt, cudaStream_t s, T* partials = nullptr,
+                                   unsigned int* counters = nullptr);
 // dense[e_k] = vals[k] for k < m (dense must be zeroed first; exponents distinct).
 template <class T>
 cudaError_t launch_scatter(T* dense, const uint64_t* idx, const T* vals, size_t m, cudaStream_t s);

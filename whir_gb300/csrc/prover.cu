@@ -78,6 +78,8 @@ struct whir_ctx {
   size_t sc_parts_bytes = 0;
   unsigned int* sc_counter = nullptr;
   unsigned int sc_launches = 0;
+  // Per-tile arrival counters of the split geometric accumulation (GR_MAX_TILES words, zeroed once).
+  unsigned int* geo_counters = nullptr;
   // Device buffers released by finished operations, kept for reuse by exact size. All of the
   // context's work is issued on its one stream, so a buffer released in stream order can be handed
   // to later work as the stream-ordered pool would, without an allocator call per buffer.
@@ -928,8 +930,10 @@ void accumulate_in_domain(whir_ctx* ctx, T* cov, size_t len, const std::vector<T
     DBuf<uint64_t> de(ctx, exps.size());
     h2d(ctx, ds.p, scalars.data(), scalars.size() * sizeof(T));
     h2d(ctx, de.p, exps.data(), exps.size() * sizeof(uint64_t));
+    const GeometricSplit sp = geometric_split_plan(len, scalars.size(), true);
+    DBuf<T> parts(ctx, sp.split && sp.groups > 1 ? sp.groups * len : 0);
     CU(launch_geometric_roots<T>(cov, len, ds.p, de.p, scalars.size(), logN, root_tab<typename T::Base>(ctx),
-                                 ctx->stream));
+                                 ctx->stream, parts.p, parts.p ? ctx->geo_counters : nullptr));
     return;
   }
   // Combine repeated query positions (indices are sampled with replacement).
@@ -1384,6 +1388,8 @@ int whir_ctx_create(int device, whir_ctx** out) {
     CU(cudaMalloc(&ctx->sc_parts, ctx->sc_parts_bytes));
     CU(cudaMalloc((void**)&ctx->sc_counter, 2 * sizeof(unsigned int)));
     CU(cudaMemset(ctx->sc_counter, 0, 2 * sizeof(unsigned int)));
+    CU(cudaMalloc((void**)&ctx->geo_counters, GR_MAX_TILES * sizeof(unsigned int)));
+    CU(cudaMemset(ctx->geo_counters, 0, GR_MAX_TILES * sizeof(unsigned int)));
     CU(cudaHostAlloc((void**)&ctx->mail_h, MAIL_DATA_OFF + MAIL_DATA_BYTES, cudaHostAllocMapped));
     memset(ctx->mail_h, 0, MAIL_DATA_OFF + MAIL_DATA_BYTES);
     CU(cudaHostGetDevicePointer((void**)&ctx->mail_d, ctx->mail_h, 0));
@@ -1415,6 +1421,7 @@ int whir_ctx_destroy(whir_ctx* ctx) {
   if (ctx->sc_parts) cudaFree(ctx->sc_parts);
   for (auto& b : ctx->free_bufs) cudaFree(b.second);
   if (ctx->sc_counter) cudaFree(ctx->sc_counter);
+  if (ctx->geo_counters) cudaFree(ctx->geo_counters);
   cudaStreamDestroy(ctx->stream);
   if (ctx->up_stream) cudaStreamDestroy(ctx->up_stream);
   delete ctx;

@@ -433,11 +433,78 @@ __global__ void __launch_bounds__(GR_THREADS) geometric_roots_kernel(T* acc, uin
   }
 }
 
+// Split form (see geometric_split_plan): thread t of a CTA takes entry t mod 2^te_log of its tile
+// and every (256 >> te_log)-th query of its group's slice; the subgroups' sums meet in shared
+// memory, then either in acc directly (one group) or through the partials and the tile's last CTA.
+template <class T>
+__global__ void __launch_bounds__(GR_THREADS) geometric_roots_split_kernel(T* acc, uint64_t n, const T* scalars,
+                                                                           const uint64_t* exps, uint64_t m,
+                                                                           int logN, RootTab rt, int te_log,
+                                                                           int groups, T* partials,
+                                                                           unsigned int* counters) {
+  typedef typename T::Base B;
+  __shared__ T red[GR_THREADS];
+  __shared__ bool am_last;
+  const int te = 1 << te_log, sg = GR_THREADS >> te_log;
+  const uint64_t tile = blockIdx.x / groups;
+  const int g = (int)(blockIdx.x - tile * groups);
+  const int e = threadIdx.x & (te - 1), sub = threadIdx.x >> te_log;
+  const uint64_t i = (tile << te_log) + e;
+  const uint64_t mask = (1ull << logN) - 1;
+  const uint64_t q0 = m * g / groups, q1 = m * (g + 1) / groups;
+  WideAcc<T> w;
+  w.init();
+  if (i < n) {
+    uint64_t j = q0 + sub;
+    // eight root-table reads issued together (their latency dominates)
+    for (; j + 7 * (uint64_t)sg < q1; j += 8 * (uint64_t)sg) {
+      B r[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) r[k] = root_pow<B>(rt, logN, (exps[j + k * sg] * i) & mask);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) w.mac_mixed(scalars[j + k * sg], r[k]);
+    }
+    for (; j < q1; j += sg) w.mac_mixed(scalars[j], root_pow<B>(rt, logN, (exps[j] * i) & mask));
+  }
+  T v = w.get();
+  if (sg > 1) {
+    red[threadIdx.x] = v;
+    __syncthreads();
+    if (sub == 0)
+      for (int t = 1; t < sg; ++t) v += red[threadIdx.x + (t << te_log)];
+  }
+  if (groups == 1) {
+    if (sub == 0 && i < n) acc[i] += v;
+    return;
+  }
+  if (sub == 0 && i < n) partials[(uint64_t)g * n + i] = v;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) am_last = atomicAdd(counters + tile, 1u) == (unsigned)groups - 1;
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  if (sub == 0 && i < n) {
+    T t = acc[i];
+    for (int gg = 0; gg < groups; ++gg) t += ldcg_t(partials + (uint64_t)gg * n + i);
+    acc[i] = t;
+  }
+  if (threadIdx.x == 0) counters[tile] = 0;
+}
+
 template <class T>
 cudaError_t launch_geometric_roots(T* acc, size_t n, const T* scalars, const uint64_t* exps, size_t m, int logN,
-                                   RootTab rt, cudaStream_t s) {
+                                   RootTab rt, cudaStream_t s, T* partials, unsigned int* counters) {
   if (n == 0 || m == 0) return cudaSuccess;
   if (logN > rt.log_order) return cudaErrorInvalidValue;
+  const GeometricSplit sp = geometric_split_plan(n, m, partials != nullptr && counters != nullptr);
+  if (sp.split) {
+    const size_t tiles = (n + ((size_t)1 << sp.te_log) - 1) >> sp.te_log;
+    geometric_roots_split_kernel<T><<<(unsigned)(tiles * sp.groups), GR_THREADS, 0, s>>>(
+        acc, n, scalars, exps, m, logN, rt, sp.te_log, sp.groups, partials, counters);
+    note_launch();
+    return cudaGetLastError();
+  }
   int E = 1;
   while (E < 8 && n / ((size_t)GR_THREADS * E * 2) >= 304) E *= 2;
   const size_t per = (size_t)GR_THREADS * E;
@@ -888,7 +955,7 @@ cudaError_t launch_univariate_eval(const S* coeffs, size_t n, T x, T* partials, 
   template cudaError_t launch_eval_eq<T>(T*, const T*, int, T, T*, cudaStream_t);                                 \
   template cudaError_t launch_geometric_accumulate<T>(T*, size_t, const T*, const T*, size_t, cudaStream_t);      \
   template cudaError_t launch_geometric_roots<T>(T*, size_t, const T*, const uint64_t*, size_t, int, RootTab,    \
-                                                 cudaStream_t);                                                  \
+                                                 cudaStream_t, T*, unsigned int*);                               \
   template cudaError_t launch_scatter<T>(T*, const uint64_t*, const T*, size_t, cudaStream_t);                   \
   template cudaError_t launch_add<T>(T*, const T*, size_t, cudaStream_t);                                        \
   template cudaError_t launch_eq_table<T>(const T*, int, int, T, T*, cudaStream_t);                              \
