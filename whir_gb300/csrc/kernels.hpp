@@ -109,6 +109,9 @@ cudaError_t launch_fold_compute(T* a, T* b, size_t n, T r, T* partials, size_t* 
 // v[i] += (v[i + n/2] - v[i]) * r for i < n/2
 template <class T>
 cudaError_t launch_fold(T* v, size_t n, T r, cudaStream_t s);
+// The same fold of two vectors of length n in one launch (the end of a sumcheck: a and b).
+template <class T>
+cudaError_t launch_fold2(T* v, T* w, size_t n, T r, cudaStream_t s);
 // Sums nparts (c0, c2) partials into out[0..2).
 template <class T>
 cudaError_t launch_reduce_pairs(const T* partials, size_t nparts, T* out, cudaStream_t s);

@@ -803,8 +803,7 @@ std::vector<T> sumcheck_device(whir_ctx* ctx, const Sumcheck& c, Transcript& ts,
   }
   {
     ProfScope prof(ctx, PF_SUMCHECK);
-    CU(launch_fold<T>(a, n, prev, ctx->stream));
-    CU(launch_fold<T>(b, n, prev, ctx->stream));
+    CU(launch_fold2<T>(a, b, n, prev, ctx->stream));
   }
   n = n > 1 ? n / 2 : n;
   return rs;
@@ -904,8 +903,7 @@ std::vector<T> initial_sumcheck_fused(whir_ctx* ctx, const Sumcheck& c, Transcri
       CU((launch_first_fold_compute_eq<T, S>(x, n, prev, tables, nforms, nvars, a, b, buf.parts.p, &np,
                                              ctx->stream)));
     } else {
-      CU(launch_fold<T>(a, n, prev, ctx->stream));
-      CU(launch_fold<T>(b, n, prev, ctx->stream));
+      CU(launch_fold2<T>(a, b, n, prev, ctx->stream));
     }
   }
   n = n > 1 ? n / 2 : n;

@@ -210,6 +210,16 @@ __global__ void __launch_bounds__(SC_THREADS) sc_fold_kernel(T* v, uint64_t n, T
 }
 
 template <class T>
+__global__ void __launch_bounds__(SC_THREADS) sc_fold2_kernel(T* v, T* w, uint64_t n, T r) {
+  const uint64_t h = n >> 1;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < h; i += (uint64_t)gridDim.x * blockDim.x) {
+    const T vlo = v[i], vhi = v[i + h], wlo = w[i], whi = w[i + h];
+    v[i] = vlo + (vhi - vlo) * r;
+    w[i] = wlo + (whi - wlo) * r;
+  }
+}
+
+template <class T>
 __global__ void __launch_bounds__(SC_THREADS) reduce_pairs_kernel(const T* partials, uint64_t nparts, T* out) {
   T s0 = T::zero(), s2 = T::zero();
   for (uint64_t i = threadIdx.x; i < nparts; i += blockDim.x) {
@@ -255,6 +265,14 @@ cudaError_t launch_fold(T* v, size_t n, T r, cudaStream_t s) {
   if (n <= 1) return cudaSuccess;
   size_t g = std::min(SC_MAX_BLOCKS, (n / 2 + SC_THREADS - 1) / SC_THREADS);
   sc_fold_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(v, n, r);
+  note_launch();
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_fold2(T* v, T* w, size_t n, T r, cudaStream_t s) {
+  if (n <= 1) return cudaSuccess;
+  size_t g = std::min(SC_MAX_BLOCKS, (n / 2 + SC_THREADS - 1) / SC_THREADS);
+  sc_fold2_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(v, w, n, r);
   note_launch();
   return cudaGetLastError();
 }
@@ -950,6 +968,7 @@ cudaError_t launch_univariate_eval(const S* coeffs, size_t n, T x, T* partials, 
                                                   unsigned int*);                                                \
   template cudaError_t launch_fold_compute<T>(T*, T*, size_t, T, T*, size_t*, cudaStream_t, T*, unsigned int*);  \
   template cudaError_t launch_fold<T>(T*, size_t, T, cudaStream_t);                                               \
+  template cudaError_t launch_fold2<T>(T*, T*, size_t, T, cudaStream_t);                                          \
   template cudaError_t launch_reduce_pairs<T>(const T*, size_t, T*, cudaStream_t);                                \
   template cudaError_t launch_reduce_singles<T>(const T*, size_t, T*, cudaStream_t);                              \
   template cudaError_t launch_eval_eq<T>(T*, const T*, int, T, T*, cudaStream_t);                                 \
