@@ -196,8 +196,17 @@ struct EncArgs {
 };
 
 // Produces whole codeword rows: writes them and (optionally) their leaf digests.
+// Minimum resident CTAs per SM for the encode kernels: three for elements of up to 16 bytes (their
+// 64 KB tiles fit three per SM; the register cap is then 85), two for the 24- and 32-byte fields
+// (without a bound the 4-limb Montgomery field took ~165 registers per thread, one CTA per SM,
+// measured 44 % slower).
+template <class F>
+struct EncMinCtas {
+  static constexpr int value = sizeof(F) <= 16 ? 3 : 2;
+};
+
 template <class F, int KIND>
-__global__ void __launch_bounds__(ENC_THREADS) encode_rows_kernel(EncArgs<F> a) {
+__global__ void __launch_bounds__(ENC_THREADS, EncMinCtas<F>::value) encode_rows_kernel(EncArgs<F> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   F* s = reinterpret_cast<F*>(smem_raw);
   const int M = a.M;
@@ -322,7 +331,7 @@ __global__ void __launch_bounds__(ENC_THREADS) encode_rows_kernel(EncArgs<F> a) 
 // Four-step pass 1: NTT_C1 over columns j2 of the (C1 x C2) view of each twisted message,
 // multiplied by w_C^(j2 k1); intermediate layout [m][c][k1][j2].
 template <class F>
-__global__ void __launch_bounds__(ENC_THREADS) encode_cols_kernel(EncArgs<F> a) {
+__global__ void __launch_bounds__(ENC_THREADS, EncMinCtas<F>::value) encode_cols_kernel(EncArgs<F> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   F* s = reinterpret_cast<F*>(smem_raw);
   const int logn = a.logC1, n = 1 << logn, W = a.W;
