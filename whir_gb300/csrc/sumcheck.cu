@@ -4,9 +4,13 @@
 
 namespace whir {
 
+// Four work items (quads of the fold-and-compute round) per thread: with one item per thread the
+// round kernels' CTAs spent most of their time in the block reduction's barriers (ncu at n = 2^20:
+// 20 % issue-active, barrier stalls first).
+static constexpr size_t SC_ITEMS_PER_THREAD = 4;
 size_t sumcheck_partials(size_t n) {
   size_t work = std::max<size_t>(n / 4, 1);
-  return std::min(SC_MAX_BLOCKS, (work + SC_THREADS - 1) / SC_THREADS);
+  return std::min(SC_MAX_BLOCKS, (work + SC_THREADS * SC_ITEMS_PER_THREAD - 1) / (SC_THREADS * SC_ITEMS_PER_THREAD));
 }
 
 WHIR_SC_INST(Gl)
