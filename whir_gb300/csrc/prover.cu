@@ -529,6 +529,17 @@ void encode_and_tree(whir_ctx* ctx, const F* d_msgs, size_t n_msgs, size_t msg_l
   std::vector<cudaEvent_t> ready;
   std::vector<size_t> bounds;
   EncodeStaging staging{1, nullptr, nullptr};
+  // If anything below throws after copies were issued, the context's stream still waits for them,
+  // so the input buffer is not handed back to the cache while a copy may be writing into it.
+  struct CopyFence {
+    whir_ctx* ctx;
+    std::vector<cudaEvent_t>* ready;
+    bool armed = true;
+    ~CopyFence() {
+      if (armed)
+        for (cudaEvent_t e : *ready) cudaStreamWaitEvent(ctx->stream, e, 0);
+    }
+  } fence{ctx, &ready};
   if (upload) {
     const size_t bytes = n_msgs * msg_len * sizeof(F);
     // Equal groups: smaller first groups (less of the copy exposed) measured slower overall, as the
@@ -557,6 +568,7 @@ void encode_and_tree(whir_ctx* ctx, const F* d_msgs, size_t n_msgs, size_t msg_l
     CU(launch_encode<F>(plan, d_msgs, n_msgs, msg_len, reinterpret_cast<F*>(w.matrix.p), w.nodes.p, kind, scratch.p,
                         root_tab<typename F::Base>(ctx), ctx->stream, upload ? &staging : nullptr));
   }
+  fence.armed = false;  // the encode enqueued the waits
   // A wait captures the event's state when it is enqueued, so the events can be reused at once.
   for (cudaEvent_t e : ready) ctx->event_pool.push_back(e);
   {
@@ -1370,7 +1382,8 @@ int whir_ctx_create(int device, whir_ctx** out) {
       throw Error(WHIR_ERR_NO_DEVICE, "no CUDA device available");
     }
     if (device < 0 || device >= count) throw Error(WHIR_ERR_INVALID, "device index out of range");
-    auto ctx = std::make_unique<whir_ctx>();
+    // Released through whir_ctx_destroy if any step below fails.
+    std::unique_ptr<whir_ctx, int (*)(whir_ctx*)> ctx(new whir_ctx(), whir_ctx_destroy);
     ctx->device = device;
     CU(cudaSetDevice(device));
     CU(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
