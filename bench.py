@@ -155,7 +155,7 @@ def evaluation(ctx, vec, point):
 
 
 def batched_and_serving(args, dev):
-    """BASELINE-style batched workload (64 Goldilocks3 polynomials, d in {14..22}) proved back to
+    """Batched workload (64 Goldilocks3 polynomials, d in {14..22}) proved back to
     back on one context and batched over several contexts, then a Poisson serving trace of Goldilocks2
     requests (d in {16..24}) at 70% of the measured batched capacity. Host wall clock (several streams
     run at once); every batched / served proof is checked byte-identical to the back-to-back one."""

@@ -1,5 +1,5 @@
 // ORACLE — test infrastructure only. CPU restatement of the WHIR reference's field arithmetic.
-// Nothing in the product library links or calls this code; it is the checker for parity tests
+// Nothing in the product library links or calls this code; parity tests compare the library with it
 // and the timed CPU baseline.
 //
 // Fields follow src/algebra/fields.rs of the reference:

@@ -120,7 +120,7 @@ def test_d20_montgomery_fields_match_oracle(ctx, orc, field):
 
 
 def test_d24_goldilocks2_verifies(ctx, orc):
-    # BASELINE workload shape: d=24 Goldilocks2, Blake3, rate 1/2, k=4, unique decoding, sec 100,
+    # Headline workload shape: d=24 Goldilocks2, Blake3, rate 1/2, k=4, unique decoding, sec 100,
     # pow 20, one random evaluation point. The oracle verifier accepts the GPU proof, and a proof
     # with a flipped bit is rejected.
     params = W.ProtocolParameters(unique_decoding=True, security_level=100, pow_bits=20)
