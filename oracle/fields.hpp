@@ -1,6 +1,6 @@
 // ORACLE — test infrastructure only. CPU restatement of the WHIR reference's field arithmetic.
-// Nothing in the product library links or calls this code; parity tests compare the library with it
-// and the timed CPU baseline.
+// Nothing in the product library links or calls this code; parity tests compare the library with
+// it, and it is the timed CPU baseline.
 //
 // Fields follow src/algebra/fields.rs of the reference:
 //   Field64   Goldilocks p = 2^64 - 2^32 + 1, generator 7                (fields.rs:85-91)
