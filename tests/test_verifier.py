@@ -56,3 +56,28 @@ def test_verifier_rejects_noncanonical_statement(orc):
     big.reshape(-1)[0] = np.uint64(0xFFFFFFFFFFFFFFFF)
     with pytest.raises(W.WhirError):
         cfg.verify("s", pr.narg, pr.hints, nw, big, covs, evals)
+
+
+def test_verifier_rejects_every_single_byte_corruption_and_truncation(orc):
+    # Robustness of the host verifier on malformed proofs: 96 single-byte corruptions spread over the
+    # proof string and the hints, truncations at arbitrary lengths and appended bytes are all
+    # rejected (WHIR_REJECT, never an exception or an acceptance).
+    case = ("Goldilocks2", 10, False, 2, 2, 10, "BLAKE3", 32, 1, 1, 1, False)
+    field, nv, ud, k, npts, powb, h, sec, bs, nw, rate, cov = case
+    cfg, op = _configs(orc, case)
+    f, vecs, pts, covs, evals = make_statement(orc, field, nv, npts, bs, nw, cov, seed=99)
+    pr = orc.whir_prove(f, op, nv, "fuzz", vecs, pts, covs, evals)
+    assert cfg.verify("fuzz", pr.narg, pr.hints, nw, pts, covs, evals)
+    rng = np.random.default_rng(5)
+    for buf_name in ("narg", "hints"):
+        buf = getattr(pr, buf_name)
+        for pos in rng.choice(len(buf), size=48, replace=False):
+            bad = bytearray(buf)
+            bad[pos] ^= int(rng.integers(1, 256))
+            args = (bytes(bad), pr.hints) if buf_name == "narg" else (pr.narg, bytes(bad))
+            assert not cfg.verify("fuzz", *args, nw, pts, covs, evals), (buf_name, int(pos))
+        for cut in sorted(set(int(c) for c in rng.integers(0, len(buf), size=8))) + [0]:
+            args = (buf[:cut], pr.hints) if buf_name == "narg" else (pr.narg, buf[:cut])
+            assert not cfg.verify("fuzz", *args, nw, pts, covs, evals), (buf_name, "cut", cut)
+        args = (buf + b"\0", pr.hints) if buf_name == "narg" else (pr.narg, buf + b"\0")
+        assert not cfg.verify("fuzz", *args, nw, pts, covs, evals), (buf_name, "appended")
