@@ -5,6 +5,7 @@ import ctypes
 import os
 import re
 
+import numpy as np
 import pytest
 
 import whir_gb300 as W
@@ -88,3 +89,32 @@ def test_no_device_fails_loudly():
     with pytest.raises(W.WhirError) as e:
         W.Context(0)
     assert e.value.code in (-4, -3)
+
+
+def test_invalid_arguments_return_error_codes():
+    # Host-side argument checks of the boundary return negative statuses (never abort): a size that is
+    # not a power of two, unknown field and engine ids, a null parameter block and a null
+    # configuration; an empty proof is a rejection, not an error.
+    lib = W.load_library()
+    p = W.ProtocolParameters(unique_decoding=True, security_level=100, pow_bits=20)
+    with pytest.raises(W.WhirError) as e:
+        W.Config("Goldilocks2", 3 << 10, p)
+    assert e.value.code < 0
+    params = W._Params()
+    params.unique_decoding = 1
+    params.starting_log_inv_rate = 1
+    params.initial_folding_factor = 4
+    params.folding_factor = 4
+    params.security_level = 100
+    params.pow_bits = 20
+    params.batch_size = 1
+    out = ctypes.c_void_p()
+    assert lib.whir_config_new(ctypes.c_int(7), ctypes.byref(params), ctypes.c_uint64(1 << 12), ctypes.byref(out)) < 0
+    params.hash_id = (ctypes.c_uint8 * 32)(*([0xAB] * 32))
+    assert lib.whir_config_new(ctypes.c_int(W.GOLDILOCKS2), ctypes.byref(params), ctypes.c_uint64(1 << 12),
+                               ctypes.byref(out)) < 0
+    assert lib.whir_config_new(ctypes.c_int(W.GOLDILOCKS2), None, ctypes.c_uint64(1 << 12), ctypes.byref(out)) < 0
+    c = W.Config("Goldilocks2", 1 << 10, p)
+    pt = np.zeros((10, 2), np.uint64)
+    assert not c.verify("s", b"", b"", 1, [pt], [], [[np.zeros(2, np.uint64)]])  # empty proof: rejected
+    assert lib.whir_verify(None, None, 0, None, 0, None, 0, 1, None, 0, None, 0, None) < 0
