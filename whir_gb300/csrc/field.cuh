@@ -29,8 +29,9 @@ static constexpr uint64_t GL_EPS = 0xFFFFFFFFULL;
 __device__ __forceinline__ uint64_t gl_add_ptx(uint64_t a, uint64_t b) {
   uint64_t r;
   // s = a + b (carry c); t = s + eps (carry c2). The canonical sum is t when c | c2, else s. The
-  // carry chains are written as multiply-adds by 1, which run on the integer multiply pipe and
-  // leave the ALU pipe (selects, compares, logic) to the rest of the field and hash code.
+  // carry chains are written as multiply-adds by 1, which moves part of the work to the integer
+  // multiply pipe: measured 6.0 ALU + 2.2 FMA-pipe instructions per add against 7.0 + 0.3 for
+  // add.cc chains (the carry-outs themselves stay on the ALU pipe).
   asm("{\n\t"
       ".reg .u32 a0, a1, b0, b1, s0, s1, t0, t1, c, c2;\n\t"
       ".reg .pred p;\n\t"
