@@ -8,9 +8,10 @@
  *     coefficient); extension elements list their base coefficients in increasing degree.
  *   - Pointers are host pointers unless a `flags` argument carries WHIR_DEVICE_PTRS, in which case
  *     the data pointers are device pointers on the context's device.
- *   - A whir_ctx owns one CUDA stream and a stream-ordered memory pool; calls on one context must
- *     not overlap (serialise them per context); different contexts may be used from different
- *     threads.
+ *   - A whir_ctx owns a CUDA stream (all kernels and results), a second stream for uploading
+ *     commit inputs from host memory while the encode runs, and a cache of device buffers in front
+ *     of the stream-ordered memory pool; calls on one context must not overlap (serialise them per
+ *     context); different contexts may be used from different threads.
  *   - There is no CPU fallback: without a usable CUDA device whir_ctx_create fails with
  *     WHIR_ERR_NO_DEVICE.
  */
