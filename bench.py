@@ -30,6 +30,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+from whir_gb300.replicas import max_over_ranks  # noqa: E402
+
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 
@@ -47,7 +49,9 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nv", type=int, default=24)
-    ap.add_argument("--cpu-nv", type=int, default=20, help="size of the bounded CPU-baseline sample")
+    ap.add_argument("--cpu-nv", type=int, default=None,
+                    help="d of the CPU-baseline proofs (default: --nv, the measured workload itself)")
+    ap.add_argument("--cpu-runs", type=int, default=5, help="timed CPU-baseline proofs (after one warm-up)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched / serving measurements")
@@ -70,15 +74,6 @@ def dist_setup(n):
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         dist.init_process_group(backend="gloo")
     return rank, world, local, dist
-
-
-def max_over_ranks(dist, x):
-    if dist is None:
-        return x
-    import torch
-    t = torch.tensor([x], dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
 
 
 def barrier(dist):
@@ -205,13 +200,23 @@ def batched_and_serving(args, dev):
     lat = srv.run(sjobs, serving.poisson_arrivals(len(sjobs), rate, seed=6))
     wall = time.perf_counter() - t
     srv.close()
+    queue = [j.start - j.arrival for j in sjobs]
+    service = [j.done - j.start for j in sjobs]
+    p99_by_d = {}
+    for d in sorted({j.nv for j in sjobs}):
+        ls = [x for x, j in zip(lat, sjobs) if j.nv == d]
+        p99_by_d[str(d)] = float(np.percentile(ls, 99)) * 1e3
     ctx.close()
     out["serving"] = {
         "workload": "%d requests, Goldilocks2 Blake3 k=4, d uniform over {16,18,20,22,24}, rate 1/2 or 1/4, 1-4 "
                     "points, unique decoding; Poisson arrivals at 70%% of measured capacity; 150 GB HBM budget"
                     % len(sjobs),
         "capacity_proofs_per_s": capacity, "arrival_rate_per_s": rate, "p50_ms": float(np.percentile(lat, 50)) * 1e3,
-        "p99_ms": float(np.percentile(lat, 99)) * 1e3, "proofs_per_s": len(sjobs) / wall, "workers": args.workers,
+        "p99_ms": float(np.percentile(lat, 99)) * 1e3,
+        "queue_p50_ms": float(np.percentile(queue, 50)) * 1e3, "queue_p99_ms": float(np.percentile(queue, 99)) * 1e3,
+        "service_p50_ms": float(np.percentile(service, 50)) * 1e3,
+        "service_p99_ms": float(np.percentile(service, 99)) * 1e3,
+        "p99_by_d_ms": p99_by_d, "proofs_per_s": len(sjobs) / wall, "workers": args.workers,
         "bit_exact_vs_plain": all((j.narg, j.hints) == r for j, r in zip(sjobs, sref)),
         "timing": "host wall clock"}
     return out
@@ -317,60 +322,67 @@ def hbm_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def cpu_baseline(args, params, vec_full, point_full):
-    """Times the oracle prover (the reference algorithm restated in C++) on a bounded sample."""
+def cpu_workload(nv):
+    """The measured workload's inputs for the oracle: the same seeded coefficients and point as
+    `workload(nv)`, and the statement's evaluation computed on the CPU."""
     import oracle
     from whir_gb300.inputs import Rng, field_elements
-    nv = args.cpu_nv
     rng = Rng(2)
     vec = rng.goldilocks(1 << nv)
     point = field_elements("Goldilocks2", nv, rng=rng).reshape(nv, 2)
     ev = oracle.multilinear_extend(oracle.GOLDILOCKS2, vec, point.reshape(-1))
     op = oracle.make_params(unique_decoding=True, security_level=100, pow_bits=20)
+    return op, vec, point, ev
+
+
+def cpu_prove(nv, op, vec, point, ev):
+    """One commit + prove of the oracle prover (the reference algorithm restated in C++, on every
+    host core). Returns (seconds, proof)."""
+    import oracle
     t0 = time.perf_counter()
-    runs = 0
-    while True:
-        oracle.whir_prove(oracle.GOLDILOCKS2, op, nv, "bench", vec.reshape(1, -1), [point], [], [[ev]])
-        runs += 1
-        if time.perf_counter() - t0 > 10.0 or runs >= 3:
-            break
-    sec = (time.perf_counter() - t0) / runs
-    scale = 1 << (args.nv - nv)
-    return {"value": sec * 1e3 * scale, "unit": "ms", "cores": oracle.lib().oracle_num_threads(), "kind": "port",
-            "sample": "%d proof(s) at d=%d (%.2f s each), scaled x%d (linear in size) to d=%d"
-                      % (runs, nv, sec, scale, args.nv)}
+    pr = oracle.whir_prove(oracle.GOLDILOCKS2, op, nv, "bench", vec.reshape(1, -1), [point], [], [[ev]])
+    return time.perf_counter() - t0, pr
+
+
+def cpu_baseline(args):
+    """Times the oracle prover on the measured workload itself (d = --cpu-nv, default --nv): one
+    warm-up proof, then --cpu-runs timed proofs; the value is their median. Also returns the first
+    proof's bytes so the GPU proof can be compared with it."""
+    import oracle
+    nv = args.cpu_nv if args.cpu_nv is not None else args.nv
+    op, vec, point, ev = cpu_workload(nv)
+    _, pr = cpu_prove(nv, op, vec, point, ev)
+    secs = [cpu_prove(nv, op, vec, point, ev)[0] for _ in range(max(1, args.cpu_runs))]
+    line = {"value": float(np.median(secs)) * 1e3, "unit": "ms", "cores": oracle.lib().oracle_num_threads(),
+            "kind": "port", "mean_ms": float(np.mean(secs)) * 1e3, "runs_ms": [t * 1e3 for t in secs],
+            "sample": "%d proof(s) at d=%d after 1 warm-up, median (the measured workload itself, no scaling)"
+                      % (len(secs), nv)}
+    return line, (pr.narg, pr.hints), nv
 
 
 def run_reference(args):
+    """The reference arm: the oracle prover (the reference's CPU algorithm, restated in C++) on all
+    host cores, one proof of the measured workload per step, --warmup untimed proofs first."""
     rank, world, local, dist = dist_setup(args.gpus)
     if rank != 0:
         return
     import oracle
-    nv = args.cpu_nv
-    from whir_gb300.inputs import Rng, field_elements
-    rng = Rng(2)
-    vec = rng.goldilocks(1 << nv)
-    point = field_elements("Goldilocks2", nv, rng=rng).reshape(nv, 2)
-    ev = oracle.multilinear_extend(oracle.GOLDILOCKS2, vec, point.reshape(-1))
-    op = oracle.make_params(unique_decoding=True, security_level=100, pow_bits=20)
+    nv = args.nv
+    op, vec, point, ev = cpu_workload(nv)
     for _ in range(args.warmup):
-        oracle.whir_prove(oracle.GOLDILOCKS2, op, nv, "bench", vec.reshape(1, -1), [point], [], [[ev]])
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        oracle.whir_prove(oracle.GOLDILOCKS2, op, nv, "bench", vec.reshape(1, -1), [point], [], [[ev]])
-    sec = (time.perf_counter() - t0) / args.steps
-    scale = 1 << (args.nv - nv)
-    ms = sec * 1e3 * scale
+        cpu_prove(nv, op, vec, point, ev)
+    secs = [cpu_prove(nv, op, vec, point, ev)[0] for _ in range(args.steps)]
+    ms = float(np.median(secs)) * 1e3
     cores = oracle.lib().oracle_num_threads()
     line = {
-        "impl": "reference", "metric": "prove_ms_d%d_goldilocks2_blake3" % args.nv, "value": ms, "unit": "ms",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "impl": "reference", "metric": "prove_ms_d%d_goldilocks2_blake3" % nv, "value": ms, "unit": "ms",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(secs)) * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks field)",
-        "data": "synthetic (SplitMix64 seed 2)",
+        "data": "synthetic (SplitMix64 seed 2, uniform field elements)",
         "config": {"workload": "WHIR PCS commit+prove d=%d Goldilocks2 Blake3 rate 1/2 k=4 sec 100 UD pow 20, 1 point"
-                               % args.nv},
+                               % nv, "statistic": "value = median of the steps, ms_per_step = their mean"},
         "cpu_baseline": {"value": ms, "unit": "ms", "cores": cores, "kind": "port",
-                         "sample": "each step: 1 proof at d=%d scaled x%d to d=%d" % (nv, scale, args.nv)},
+                         "sample": "each step: 1 proof at d=%d (the measured workload itself, no scaling)" % nv},
         "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -411,6 +423,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
 
     times = []
+    first_timed_proof = None
     launches0 = ctx.launch_count()
     sampler = ClockSampler(dev)
     sampler.start()
@@ -424,7 +437,10 @@ def run_gpu(args):
         e1.record(stream)
         e1.synchronize()
         times.append(e0.elapsed_time(e1))
-        assert ps.proof() == ref_narg, "proof bytes changed between runs"
+        proof = ps.proof()
+        assert proof == ref_narg, "proof bytes changed between runs"
+        if first_timed_proof is None:
+            first_timed_proof = proof
     clocks = sampler.stop()
     launches = ctx.launch_count() - launches0
     # Per-family device time (CUDA events around each kernel family on the context's stream), taken
@@ -486,7 +502,10 @@ def run_gpu(args):
     else:
         roofline = {"bound": "integer", "kernel_family": fam, "achieved": None, "peak": peak, "unit": "GB/s",
                     "frac": None, "traffic": None, "avg_launch_ms": ms_f / calls_f}
-    cpu = None if args.no_cpu_baseline else cpu_baseline(args, params, vec, point)
+    cpu, bit_exact = None, None
+    if not args.no_cpu_baseline:
+        cpu, cpu_proof, cpu_nv = cpu_baseline(args)
+        bit_exact = (cpu_proof == first_timed_proof) if cpu_nv == nv else None
     extra = {} if args.no_batch else batched_and_serving(args, dev)
     if not args.no_multilimb:
         extra["multilimb"] = multilimb(args, dev)
@@ -502,6 +521,7 @@ def run_gpu(args):
         "roofline": roofline,
         "kernel_families_ms_per_proof": {k: v[0] / prof_steps for k, v in prof.items() if v[1]},
         "cpu_baseline": cpu,
+        "bit_exact_vs_cpu": bit_exact,
         "e2e": e2e,
         "gpu_launches": int(launches),
         "clocks": clocks,

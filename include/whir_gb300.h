@@ -179,6 +179,10 @@ int whir_geometric_accumulate(whir_ctx* ctx, int field, uint64_t* acc, size_t n,
 /* mixed_univariate_evaluate (src/algebra/mod.rs:105-129) for the embedding `field`. */
 int whir_univariate_evaluate(whir_ctx* ctx, int field, const uint64_t* coeffs, size_t n, const uint64_t* point,
                              uint64_t* out, uint32_t flags);
+/* lift (src/algebra/mod.rs:51-59): dst[i] = embedding.map(src[i]) for the embedding `field`
+ * (n source elements in, n target elements out; Goldilocks2/3 put the value in the constant
+ * coefficient). */
+int whir_lift(whir_ctx* ctx, int field, const uint64_t* src, size_t n, uint64_t* dst, uint32_t flags);
 /* Evaluation of the multilinear extension of n <= 2^nvars source values (implicitly zero-padded)
  * at a target-field point: MultilinearExtension's Evaluate (linear_form/multilinear_extension.rs:
  * 53-57 -> mixed_multilinear_extend, src/algebra/multilinear.rs:15-151). This is how callers compute
@@ -199,10 +203,14 @@ int whir_pow_grind(whir_ctx* ctx, const uint8_t engine_id[32], const uint8_t cha
  * stream is a cudaStream_t (NULL = legacy default stream); the work is only enqueued.
  *   - Scratch: the two eq tables live in one file-scope device array of
  *     whir_eval_eq_noalloc_max_scratch() bytes (256 KiB), held on every device that loads the
- *     library until the process exits; nvars is limited to what fits (<= 26 for Goldilocks2,
- *     <= 24 for Goldilocks3) and larger nvars (or nvars == 0) is rejected with WHIR_ERR_INVALID.
- *   - The first call on each device looks up the array's device address (cudaGetSymbolAddress,
- *     with that device current); make that first call before any stream capture.
+ *     library until the process exits; nvars is limited to what fits,
+ *     (2^ceil(nvars/2) + 2^floor(nvars/2)) * element bytes <= 256 KiB: nvars <= 28 for Goldilocks1,
+ *     <= 26 for Goldilocks2, <= 24 for Goldilocks3. Larger nvars (or nvars == 0) is rejected with
+ *     WHIR_ERR_INVALID.
+ *   - Each call made outside a stream capture looks up the array's device address on the current
+ *     device (cudaGetSymbolAddress); a call made while `stream` is capturing reuses the address of
+ *     the last such call on that device, so make one call on each device before any capture (and
+ *     again after a device reset).
  *   - All calls share the array and it keeps the last call's tables; every call rewrites the
  *     tables before reading them. Calls whose work overlaps on the GPU (different streams, or
  *     different host threads on the same device) race on the array: serialise them.

@@ -111,8 +111,9 @@ def main(root):
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    data = main(root)
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_reference_kats.py <root of the reference crate's sources>")
+    data = main(sys.argv[1])
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_kats.json")
     with open(path, "w") as f:
         json.dump(data, f, indent=1)

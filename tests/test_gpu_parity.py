@@ -96,6 +96,21 @@ def test_encode_d24_initial_shape_properties(ctx, orc):
             assert int(cw[r, m]) == int(v[0])
 
 
+@pytest.mark.parametrize("fname,fid", FIELDS)
+@pytest.mark.parametrize("n", [1, 7, 4096, 100003])
+def test_lift_parity(ctx, orc, fid, fname, n):
+    # lift maps each source element into the target field (Embedding::map, embedding.rs:141-153):
+    # the constant coefficient of a Goldilocks extension with zeros above it, the identity for the
+    # prime fields (canonical limbs in and out, also for the Montgomery-form fields).
+    rng = Rng(n + 5 * fid)
+    src = field_elements(BASE_NAME[fname], n, rng=rng).reshape(n, -1)
+    got = W.lift(ctx, fid, src).reshape(n, -1)
+    L, S = W.TARGET_LIMBS[fid], W.SOURCE_LIMBS[fid]
+    want = np.zeros((n, L), np.uint64)
+    want[:, :S] = src
+    assert np.array_equal(got, want)
+
+
 @pytest.mark.parametrize("engine", ["Blake3", "Sha2", "Sha3", "Keccak"])
 @pytest.mark.parametrize("size", [0, 4, 32, 60, 64, 128, 132, 256, 384, 512, 1020, 1024])
 def test_hash_many_parity(ctx, orc, engine, size):

@@ -119,10 +119,11 @@ def test_d20_montgomery_fields_match_oracle(ctx, orc, field):
     assert orc.whir_verify(f, op, 20, "d20 " + field, 1, narg, hints, pts, [], evs)
 
 
-def test_d24_goldilocks2_verifies(ctx, orc):
-    # Headline workload shape: d=24 Goldilocks2, Blake3, rate 1/2, k=4, unique decoding, sec 100,
-    # pow 20, one random evaluation point. The oracle verifier accepts the GPU proof, and a proof
-    # with a flipped bit is rejected.
+def test_d24_goldilocks2_matches_oracle_and_verifies(ctx, orc):
+    # Headline workload: d=24 Goldilocks2, Blake3, rate 1/2, k=4, unique decoding, sec 100, pow 20,
+    # one random evaluation point (the seed the benchmark uses). The GPU proof is byte-identical to
+    # the oracle prover's (roots, NARG string, hints, final claim), both verifiers accept it, and a
+    # proof with a flipped bit is rejected.
     params = W.ProtocolParameters(unique_decoding=True, security_level=100, pow_bits=20)
     op = orc.make_params(unique_decoding=True, security_level=100, pow_bits=20)
     r = Rng(2)
@@ -130,6 +131,12 @@ def test_d24_goldilocks2_verifies(ctx, orc):
     pt = field_elements("Goldilocks2", 24, rng=r).reshape(24, 2)
     ev = orc.multilinear_extend(orc.GOLDILOCKS2, vec.reshape(-1), pt.reshape(-1))
     narg, hints, claim, roots = gpu_prove(ctx, "Goldilocks2", params, 24, "d24", vec, [pt], [], [[ev]], 1)
+    ref = orc.whir_prove(orc.GOLDILOCKS2, op, 24, "d24", vec, [pt], [], [[ev]])
+    assert b"".join(roots) == ref.roots
+    assert narg == ref.narg
+    assert hints == ref.hints
+    assert np.array_equal(claim.evaluation_point.reshape(-1), ref.evaluation_point)
+    assert np.array_equal(claim.rlc_coefficients.reshape(-1), ref.rlc_coefficients)
     assert orc.whir_verify(orc.GOLDILOCKS2, op, 24, "d24", 1, narg, hints, [pt], [], [[ev]])
     cfg = W.Config("Goldilocks2", 1 << 24, params)
     assert cfg.verify("d24", narg, hints, 1, [pt], [], [[ev]])

@@ -57,17 +57,60 @@ def test_noalloc_eval_eq_matches_regular_entry_point(fname, fid, nvars):
         ctx.close()
 
 
-def test_noalloc_rejects_sizes_beyond_its_scratch():
+@pytest.mark.parametrize("fname,fid,max_nvars", [("Goldilocks1", W.GOLDILOCKS1, 28), ("Goldilocks2", W.GOLDILOCKS2, 26),
+                                                 ("Goldilocks3", W.GOLDILOCKS3, 24)])
+def test_noalloc_size_limits(fname, fid, max_nvars):
+    # The largest nvars whose eq tables fit the 256 KiB scratch is accepted and agrees bit for bit
+    # with whir_eval_eq on the same device buffers; one more variable is rejected before any work.
+    torch = pytest.importorskip("torch")
     lib = W.load_library()
     lib.whir_eval_eq_noalloc_max_scratch.restype = ctypes.c_size_t
     assert lib.whir_eval_eq_noalloc_max_scratch() == 256 * 1024
+    L = W.TARGET_LIMBS[fid]
+    rng = Rng(500 + fid)
+    point = torch.from_numpy(field_elements(fname, max_nvars, rng=rng).reshape(-1).view(np.int64)).cuda()
+    scalar = field_elements(fname, 1, rng=rng).reshape(-1)
+    gen = torch.Generator(device="cuda").manual_seed(fid)
+    acc = torch.randint(0, 1 << 62, ((1 << max_nvars) * L,), dtype=torch.int64, device="cuda", generator=gen)
+    ref = acc.clone()
+    torch.cuda.synchronize()
     ctx = W.Context(0)
     try:
-        dummy = ctx.alloc(64)
+        rc, err = _noalloc(lib, fid, acc.data_ptr(), point.data_ptr(), max_nvars, scalar, ctx.stream_handle())
+        assert rc == 0, err
+        s = np.ascontiguousarray(scalar, dtype=np.uint64)
+        rc = lib.whir_eval_eq(ctx._h, ctypes.c_int(fid), ctypes.c_void_p(ref.data_ptr()),
+                              ctypes.c_void_p(point.data_ptr()), ctypes.c_size_t(max_nvars),
+                              s.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), ctypes.c_uint32(W.DEVICE_PTRS))
+        assert rc == 0, lib.whir_last_error().decode()
+        ctx.synchronize()
+        assert torch.equal(acc, ref)
+        before = acc.clone()
+        torch.cuda.synchronize()
+        rc, err = _noalloc(lib, fid, acc.data_ptr(), point.data_ptr(), max_nvars + 1, scalar, ctx.stream_handle())
+        assert rc == -1 and "scratch" in err
+        ctx.synchronize()
+        assert torch.equal(acc, before)
+        rc, err = _noalloc(lib, fid, acc.data_ptr(), point.data_ptr(), 1, scalar, ctx.stream_handle())
+        assert rc == 0 and err == "", "a successful call leaves no error message behind"
+        ctx.synchronize()
+    finally:
+        ctx.close()
+
+
+def test_noalloc_rejects_bad_arguments():
+    lib = W.load_library()
+    ctx = W.Context(0)
+    dummy = ctx.alloc(64)
+    try:
         rc, err = _noalloc(lib, W.GOLDILOCKS3, dummy, dummy, 27, np.zeros(3, np.uint64), ctx.stream_handle())
         assert rc == -1 and "scratch" in err
-        ctx.free(dummy)
+        rc, err = _noalloc(lib, W.GOLDILOCKS2, dummy, dummy, 0, np.zeros(2, np.uint64), ctx.stream_handle())
+        assert rc == -1
+        rc, err = _noalloc(lib, W.FIELD192, dummy, dummy, 2, np.zeros(3, np.uint64), ctx.stream_handle())
+        assert rc == -1 and "field" in err
     finally:
+        ctx.free(dummy)
         ctx.close()
 
 

@@ -469,6 +469,16 @@ def univariate_evaluate(ctx, field, coeffs, point):
     return out
 
 
+def lift(ctx, field, src):
+    """lift (algebra/mod.rs:51-59): source elements of the embedding -> target elements."""
+    s = _as_u64(src).reshape(-1)
+    n = s.size // SOURCE_LIMBS[field]
+    out = np.zeros(max(n, 1) * TARGET_LIMBS[field], dtype=np.uint64)
+    _check(load_library().whir_lift(ctx._h, ctypes.c_int(field), _u64ptr(s), ctypes.c_size_t(n), _u64ptr(out),
+                                    ctypes.c_uint32(0)))
+    return out[: n * TARGET_LIMBS[field]]
+
+
 def multilinear_evaluate(ctx, field, coeffs, point):
     """MultilinearExtension(point).evaluate(embedding, coeffs) on the device."""
     c = _as_u64(coeffs).reshape(-1)

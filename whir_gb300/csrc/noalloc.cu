@@ -8,8 +8,8 @@
 //
 // The scratch array lives for as long as the library is loaded, on every device that loads it.
 // Host code cannot use the array's name as a device address (in host code the symbol is only a
-// host-side stand-in), so the device address is looked up once per device with
-// cudaGetSymbolAddress, with that device current, during the first call made on that device.
+// host-side stand-in), so the device address is looked up with cudaGetSymbolAddress, with the
+// device current, by each call made outside a stream capture.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -35,14 +35,22 @@ int fail(int code, const std::string& m) {
   return code;
 }
 
-// Device address of the scratch array on the current device (looked up once per device).
-int scratch_address(int device, void** out) {
+// Device address of the scratch array on the current device. Looked up again on every call made
+// outside a stream capture (the lookup is cheap, and a fresh one stays valid after a device reset or
+// in a context other than the one of an earlier call); a call made while `stream` is capturing uses
+// the address found by the last call on this device that was not capturing.
+int scratch_address(int device, cudaStream_t stream, void** out) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  const cudaError_t qe = cudaStreamIsCapturing(stream, &cs);
+  if (qe != cudaSuccess) cudaGetLastError();  // the query's error must not reach the launch check
   std::lock_guard<std::mutex> g(g_mu);
-  if (!g_scratch_ptr[device]) {
+  if (qe == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return fail(WHIR_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     g_scratch_ptr[device] = p;
+  } else if (!g_scratch_ptr[device]) {
+    return fail(WHIR_ERR_INVALID, "the first call on a device must be made outside a stream capture");
   }
   *out = g_scratch_ptr[device];
   return 0;
@@ -77,16 +85,17 @@ size_t whir_eval_eq_noalloc_max_scratch(void) { return NOALLOC_SCRATCH_BYTES; }
 
 int whir_eval_eq_noalloc(int field, uint64_t* acc_dev, const uint64_t* point_dev, size_t nvars,
                          const uint64_t* scalar, void* stream) {
+  g_err.clear();
   if (!acc_dev || !scalar || (nvars > 0 && !point_dev)) return fail(WHIR_ERR_INVALID, "null argument");
   if (nvars == 0 || nvars > 62) return fail(WHIR_ERR_INVALID, "nvars must be in [1, 62]");
   int device = -1;
   cudaError_t e = cudaGetDevice(&device);
   if (e != cudaSuccess) return fail(WHIR_ERR_NO_DEVICE, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   if (device < 0 || device >= MAX_DEVICES) return fail(WHIR_ERR_INVALID, "device index out of range");
-  void* scratch = nullptr;
-  int rc = scratch_address(device, &scratch);
-  if (rc) return rc;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  void* scratch = nullptr;
+  int rc = scratch_address(device, s, &scratch);
+  if (rc) return rc;
   switch (field) {
     case WHIR_GOLDILOCKS1: return run<whir::Gl>(acc_dev, point_dev, nvars, scalar, s, scratch);
     case WHIR_GOLDILOCKS2: return run<whir::Gl2>(acc_dev, point_dev, nvars, scalar, s, scratch);

@@ -1910,6 +1910,31 @@ int whir_univariate_evaluate(whir_ctx* ctx, int field, const uint64_t* coeffs, s
   });
 }
 
+int whir_lift(whir_ctx* ctx, int field, const uint64_t* src, size_t n, uint64_t* dst, uint32_t flags) {
+  return guarded([&] {
+    check_ctx(ctx);
+    if (n && (!src || !dst)) throw Error(WHIR_ERR_INVALID, "null argument");
+    return with_embedding(field, [&]<class S, class T>() {
+      if (n == 0) return 0;
+      const bool dev = (flags & WHIR_DEVICE_PTRS) != 0;
+      DBuf<S> hs;
+      DBuf<T> own;
+      const S* ds = device_vectors<S>(ctx, src, n, flags, hs);
+      T* dd = dev ? reinterpret_cast<T*>(dst) : (own = DBuf<T>(ctx, n)).p;
+      const S* vecs[1] = {ds};
+      const T coeffs[1] = {T::one()};
+      CU((launch_lift_rlc<T, S>(dd, vecs, coeffs, 1, n, ctx->stream)));
+      CU(launch_to_canonical<T>(dd, n, ctx->stream));
+      if (!dev) {
+        ctx->d2h_bytes += n * sizeof(T);
+        CU(cudaMemcpyAsync(dst, dd, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+      }
+      CU(cudaStreamSynchronize(ctx->stream));
+      return 0;
+    });
+  });
+}
+
 int whir_multilinear_evaluate(whir_ctx* ctx, int field, const uint64_t* coeffs, size_t n, const uint64_t* point,
                               size_t nvars, uint64_t* out, uint32_t flags) {
   return guarded([&] {

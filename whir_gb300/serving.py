@@ -42,7 +42,8 @@ class ProofJob:
         self.session = session
         self.narg = None
         self.hints = None
-        self.arrival = None
+        self.arrival = None  # request arrival (host clock, set by ProofServer)
+        self.start = None  # picked up by a worker
         self.done = None
 
     @property
@@ -135,7 +136,9 @@ class ProofServer:
 
     def run(self, jobs, arrivals):
         """Replays a request trace: job i arrives `arrivals[i]` seconds after the start. Returns
-        per-job latencies in seconds (completion - arrival) in job order."""
+        per-job latencies in seconds (completion - arrival) in job order; each job also keeps its
+        arrival, start (picked up by a worker) and completion times, so latency splits into queueing
+        (start - arrival) and service (done - start)."""
         n = len(jobs)
         est = [j.memory_estimate() for j in jobs]
         if any(e > self.budget for e in est):
@@ -172,6 +175,7 @@ class ProofServer:
                         return  # failed elsewhere, or every job has been taken
                     i = admitted.popleft()
                     state["taken"] += 1
+                    jobs[i].start = time.perf_counter()
                 try:
                     prove_job(ctx, jobs[i])
                 except Exception as e:
