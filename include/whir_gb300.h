@@ -101,6 +101,10 @@ int whir_config_free(whir_config* cfg);
 /* JSON summary of the derived round schedule (sizes, sample counts, PoW thresholds). */
 int whir_config_json(const whir_config* cfg, char* buf, size_t cap);
 
+/* ciborium::into_writer(&config): the CBOR of the serde form of whir::Config
+ * (src/transcript/mod.rs:111-121, src/protocols/whir/mod.rs:29-46), whose SHA3-512 is the
+ * protocol id. Writes up to cap bytes to buf (nullable) and the full length to *len. */
+int whir_config_cbor(const whir_config* cfg, uint8_t* buf, size_t cap, size_t* len);
 /* ProverState::new_std(&DomainSeparator::protocol(&config).session(&session).instance(&Empty))
  * (src/transcript/mod.rs:110-181). */
 int whir_prover_state_new(const whir_config* cfg, const char* session, size_t session_len,

@@ -352,55 +352,191 @@ WhirConfig whir_config_new(size_t size, const ProtocolParameters& wp, double fie
   return cfg;
 }
 
-static void put_u64(std::vector<uint8_t>& o, uint64_t v) {
-  for (int i = 0; i < 8; ++i) o.push_back((uint8_t)(v >> (8 * i)));
-}
-static void put_bytes(std::vector<uint8_t>& o, const uint8_t* b, size_t n) { o.insert(o.end(), b, b + n); }
-static void put_irs(std::vector<uint8_t>& o, const IrsConfig& c) {
-  put_u64(o, c.num_vectors);
-  put_u64(o, c.vector_size);
-  put_u64(o, c.mask_length);
-  put_u64(o, c.codeword_length);
-  put_u64(o, c.interleaving_depth);
-  put_u64(o, c.num_cols);
-  put_bytes(o, c.leaf_hash_id, 32);
-  put_u64(o, c.merkle.num_leaves);
-  put_u64(o, c.merkle.layers);
-  put_bytes(o, c.merkle.hash_id, 32);
-  uint64_t js;
-  memcpy(&js, &c.johnson_slack, 8);
-  put_u64(o, js);
-  put_u64(o, c.in_domain_samples);
-  put_u64(o, c.out_domain_samples);
-  put_u64(o, c.deduplicate_in_domain ? 1 : 0);
-}
-static void put_pow(std::vector<uint8_t>& o, const PowConfig& p) {
-  put_bytes(o, p.hash_id, 32);
-  put_u64(o, p.threshold);
-}
-static void put_sc(std::vector<uint8_t>& o, const SumcheckConfig& s) {
-  put_u64(o, s.initial_size);
-  put_pow(o, s.round_pow);
-  put_u64(o, s.num_rounds);
-  put_u64(o, s.mask_length);
+// ---- protocol id bytes: ciborium::into_writer(&whir::Config) (transcript/mod.rs:111-121) -------
+// The configuration is first built as a tree of serde data-model values (protocols/whir/mod.rs:
+// 29-46, irs_commit.rs:51-91, matrix_commit.rs:93-111, merkle_tree.rs:25-40, sumcheck.rs:33-44,
+// proof_of_work.rs:23-27, type_info.rs:98-117, fields.rs:32-62, embedding.rs:43-59, 191-205), then
+// written as CBOR (RFC 8949) the way ciborium does: shortest heads, definite lengths, floats in the
+// shortest IEEE width that holds the value exactly.
+namespace {
+struct Sv {  // serde value
+  enum Kind { UINT, BOOL, FLOAT, BYTES, TEXT, SEQ, STRUCT } kind;
+  uint64_t u = 0;
+  double f = 0;
+  std::string s;                                  // text, or bytes
+  std::vector<Sv> items;                          // sequence elements / struct field values
+  std::vector<std::string> names;                 // struct field names
+  static Sv uint(uint64_t v) { Sv x{UINT}; x.u = v; return x; }
+  static Sv boolean(bool v) { Sv x{BOOL}; x.u = v; return x; }
+  static Sv real(double v) { Sv x{FLOAT}; x.f = v; return x; }
+  static Sv text(const std::string& t) { Sv x{TEXT}; x.s = t; return x; }
+  static Sv bytes(const std::vector<uint8_t>& b) { Sv x{BYTES}; x.s.assign(b.begin(), b.end()); return x; }
+  static Sv seq(std::vector<Sv> v) { Sv x{SEQ}; x.items = std::move(v); return x; }
+  static Sv record(std::vector<std::pair<std::string, Sv>> fields) {
+    Sv x{STRUCT};
+    for (auto& f : fields) {
+      x.names.push_back(f.first);
+      x.items.push_back(std::move(f.second));
+    }
+    return x;
+  }
+};
+
+void cbor_head(std::vector<uint8_t>& o, int major, uint64_t v) {
+  int extra = v < 24 ? 0 : v < (1ull << 8) ? 1 : v < (1ull << 16) ? 2 : v < (1ull << 32) ? 4 : 8;
+  int info = extra == 0 ? (int)v : extra == 1 ? 24 : extra == 2 ? 25 : extra == 4 ? 26 : 27;
+  o.push_back((uint8_t)((major << 5) | info));
+  for (int i = extra - 1; i >= 0; --i) o.push_back((uint8_t)(v >> (8 * i)));
 }
 
-std::vector<uint8_t> config_bytes(const WhirConfig& c, int field_kind) {
-  std::vector<uint8_t> o;
-  const char* tag = "whir-gb300 config v1";
-  put_bytes(o, (const uint8_t*)tag, strlen(tag));
-  put_u64(o, (uint64_t)field_kind);
-  put_irs(o, c.initial_committer);
-  put_sc(o, c.initial_sumcheck);
-  put_pow(o, c.initial_skip_pow);
-  put_u64(o, c.rounds.size());
-  for (auto& r : c.rounds) {
-    put_irs(o, r.irs);
-    put_sc(o, r.sumcheck);
-    put_pow(o, r.pow);
+// IEEE binary16 bit pattern of v if it holds v exactly.
+bool half_exact(double v, uint16_t& out) {
+  uint64_t b;
+  memcpy(&b, &v, 8);
+  const uint64_t sign = b >> 63;
+  const int exp = (int)((b >> 52) & 0x7ff);
+  const uint64_t man = b & ((1ull << 52) - 1);
+  if (exp == 0x7ff) return false;  // not produced by the configuration
+  if (exp == 0 && man == 0) {
+    out = (uint16_t)(sign << 15);
+    return true;
   }
-  put_sc(o, c.final_sumcheck);
-  put_pow(o, c.final_pow);
+  if (exp == 0) return false;  // binary64 subnormals are far below binary16's range
+  const int e = exp - 1023;  // v = 1.man * 2^e
+  if (e >= -14 && e <= 15) {
+    if (man & ((1ull << 42) - 1)) return false;  // more than 10 mantissa bits
+    out = (uint16_t)((sign << 15) | ((uint64_t)(e + 15) << 10) | (man >> 42));
+    return true;
+  }
+  if (e >= -24 && e < -14) {  // binary16 subnormal: v = k * 2^-24
+    const uint64_t full = man | (1ull << 52);
+    const int shift = 52 - (e + 24);  // k = full >> shift
+    if (full & ((1ull << shift) - 1)) return false;
+    out = (uint16_t)((sign << 15) | (full >> shift));
+    return true;
+  }
+  return false;
+}
+
+void cbor_write(std::vector<uint8_t>& o, const Sv& v) {
+  switch (v.kind) {
+    case Sv::UINT: cbor_head(o, 0, v.u); break;
+    case Sv::BOOL: o.push_back(v.u ? 0xf5 : 0xf4); break;
+    case Sv::BYTES:
+    case Sv::TEXT:
+      cbor_head(o, v.kind == Sv::BYTES ? 2 : 3, v.s.size());
+      o.insert(o.end(), v.s.begin(), v.s.end());
+      break;
+    case Sv::SEQ:
+      cbor_head(o, 4, v.items.size());
+      for (const Sv& x : v.items) cbor_write(o, x);
+      break;
+    case Sv::STRUCT:
+      cbor_head(o, 5, v.items.size());
+      for (size_t i = 0; i < v.items.size(); ++i) {
+        cbor_write(o, Sv::text(v.names[i]));
+        cbor_write(o, v.items[i]);
+      }
+      break;
+    case Sv::FLOAT: {
+      uint16_t h;
+      const float f = (float)v.f;
+      if (half_exact(v.f, h)) {
+        o.push_back(0xf9);
+        o.push_back((uint8_t)(h >> 8));
+        o.push_back((uint8_t)h);
+      } else if ((double)f == v.f) {
+        uint32_t b;
+        memcpy(&b, &f, 4);
+        o.push_back(0xfa);
+        for (int i = 3; i >= 0; --i) o.push_back((uint8_t)(b >> (8 * i)));
+      } else {
+        uint64_t b;
+        memcpy(&b, &v.f, 8);
+        o.push_back(0xfb);
+        for (int i = 7; i >= 0; --i) o.push_back((uint8_t)(b >> (8 * i)));
+      }
+      break;
+    }
+  }
+}
+
+Sv engine_sv(const uint8_t* id) {
+  std::vector<Sv> v;
+  for (int i = 0; i < 32; ++i) v.push_back(Sv::uint(id[i]));
+  return Sv::seq(std::move(v));
+}
+// FieldInfo of a field whose characteristic is the oracle's field `kind` base prime.
+Sv field_info_sv(int kind, uint64_t degree) {
+  std::vector<uint64_t> limbs;
+  if (kind == ORACLE_FIELD192) {
+    limbs.assign(f192_params().p, f192_params().p + 3);
+  } else if (kind == ORACLE_FIELD256) {
+    limbs.assign(f256_params().p, f256_params().p + 4);
+  } else {
+    limbs.push_back(GL_P);
+  }
+  std::vector<uint8_t> be;
+  for (size_t i = limbs.size(); i-- > 0;)
+    for (int b = 7; b >= 0; --b) be.push_back((uint8_t)(limbs[i] >> (8 * b)));
+  size_t lead = 0;
+  while (lead < be.size() && be[lead] == 0) ++lead;
+  be.erase(be.begin(), be.begin() + lead);
+  return Sv::record({{"characteristic", Sv::bytes(be)}, {"extension_degree", Sv::uint(degree)}});
+}
+uint64_t target_degree(int kind) { return kind == ORACLE_GOLDILOCKS2 ? 2 : kind == ORACLE_GOLDILOCKS3 ? 3 : 1; }
+
+Sv pow_sv(const PowConfig& p) {
+  return Sv::record({{"hash_id", engine_sv(p.hash_id)}, {"threshold", Sv::uint(p.threshold)}});
+}
+Sv sumcheck_sv(const SumcheckConfig& s, int kind) {
+  return Sv::record({{"field", field_info_sv(kind, target_degree(kind))},
+                     {"initial_size", Sv::uint(s.initial_size)},
+                     {"round_pow", pow_sv(s.round_pow)},
+                     {"num_rounds", Sv::uint(s.num_rounds)},
+                     {"mask_length", Sv::uint(s.mask_length)}});
+}
+// identity = true: irs_commit::Config<Identity<Target>>; else the config's own embedding.
+Sv irs_sv(const IrsConfig& c, int kind, bool identity) {
+  const uint64_t deg = target_degree(kind);
+  const bool base = !identity && deg > 1;
+  Sv emb = Sv::record({{"type", Sv::text(base ? "basefield" : "identity")},
+                       {"value", Sv::record({{base ? "extension" : "field", field_info_sv(kind, deg)}})}});
+  std::vector<Sv> layers;
+  for (size_t l = 0; l < c.merkle.layers; ++l) layers.push_back(Sv::record({{"hash_id", engine_sv(c.merkle.hash_id)}}));
+  Sv merkle = Sv::record({{"num_leaves", Sv::uint(c.merkle.num_leaves)}, {"layers", Sv::seq(std::move(layers))}});
+  Sv matrix = Sv::record({{"element_type", field_info_sv(kind, base ? 1 : deg)},
+                          {"num_cols", Sv::uint(c.num_cols)},
+                          {"leaf_hash_id", engine_sv(c.leaf_hash_id)},
+                          {"merkle_tree", std::move(merkle)}});
+  return Sv::record({{"embedding", std::move(emb)},
+                     {"num_vectors", Sv::uint(c.num_vectors)},
+                     {"vector_size", Sv::uint(c.vector_size)},
+                     {"mask_length", Sv::uint(c.mask_length)},
+                     {"codeword_length", Sv::uint(c.codeword_length)},
+                     {"interleaving_depth", Sv::uint(c.interleaving_depth)},
+                     {"matrix_commit", std::move(matrix)},
+                     {"johnson_slack", Sv::real(c.johnson_slack)},
+                     {"in_domain_samples", Sv::uint(c.in_domain_samples)},
+                     {"out_domain_samples", Sv::uint(c.out_domain_samples)},
+                     {"deduplicate_in_domain", Sv::boolean(c.deduplicate_in_domain)}});
+}
+}  // namespace
+
+std::vector<uint8_t> config_bytes(const WhirConfig& c, int field_kind) {
+  std::vector<Sv> rounds;
+  for (const auto& r : c.rounds)
+    rounds.push_back(Sv::record({{"irs_committer", irs_sv(r.irs, field_kind, true)},
+                                 {"sumcheck", sumcheck_sv(r.sumcheck, field_kind)},
+                                 {"pow", pow_sv(r.pow)}}));
+  Sv cfg = Sv::record({{"initial_committer", irs_sv(c.initial_committer, field_kind, false)},
+                       {"initial_sumcheck", sumcheck_sv(c.initial_sumcheck, field_kind)},
+                       {"initial_skip_pow", pow_sv(c.initial_skip_pow)},
+                       {"round_configs", Sv::seq(std::move(rounds))},
+                       {"final_sumcheck", sumcheck_sv(c.final_sumcheck, field_kind)},
+                       {"final_pow", pow_sv(c.final_pow)}});
+  std::vector<uint8_t> o;
+  cbor_write(o, cfg);
   return o;
 }
 

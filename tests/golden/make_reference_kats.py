@@ -64,6 +64,71 @@ def challenge_index_cases(lines):
     return cases
 
 
+def struct_fields(lines, name, after=0):
+    """Field names, in declaration order, of the first `struct <name>` at or after line `after`,
+    with serde renames applied (the names serde writes as map keys), and the struct's line."""
+    i = after
+    while i < len(lines):
+        if re.match(r"\s*(pub\s+)?struct\s+%s\b" % name, lines[i]) and "(" not in lines[i].split(name, 1)[1][:2]:
+            break
+        i += 1
+    else:
+        raise KeyError(name)
+    start = i
+    while "{" not in lines[i]:
+        i += 1
+    fields, rename = [], None
+    i += 1
+    while not lines[i].strip().startswith("}"):
+        ln = lines[i].strip()
+        m = re.search(r'#\[serde\(rename = "([^"]+)"\)\]', ln)
+        if m:
+            rename = m.group(1)
+        m = re.match(r"(pub\s+)?(\w+)\s*:", ln)
+        if m and not ln.startswith("//") and not ln.startswith("#"):
+            fields.append(rename or m.group(2))
+            rename = None
+        i += 1
+    return fields, start + 1
+
+
+def type_info_string(lines, embedding):
+    """The TypeInfo string of an embedding type (`impl ... TypeInfo for <embedding><F>`)."""
+    for i, ln in enumerate(lines):
+        if re.search(r"impl<.*> TypeInfo for %s<" % embedding, ln):
+            for j in range(i, i + 8):
+                m = re.search(r'"(\w+)"\.into\(\)', lines[j])
+                if m:
+                    return m.group(1), j + 1
+    raise KeyError(embedding)
+
+
+def serde_layout(root):
+    """Field names and order of every serde struct in whir::Config's serialized form (the CBOR map
+    keys ciborium writes for the protocol id), with the file:line of each struct."""
+    specs = [("whir_config", "src/protocols/whir/mod.rs", "Config"),
+             ("round_config", "src/protocols/whir/mod.rs", "RoundConfig"),
+             ("irs_config", "src/protocols/irs_commit.rs", "Config"),
+             ("matrix_config", "src/protocols/matrix_commit.rs", "Config"),
+             ("merkle_config", "src/protocols/merkle_tree.rs", "Config"),
+             ("merkle_layer", "src/protocols/merkle_tree.rs", "LayerConfig"),
+             ("sumcheck_config", "src/protocols/sumcheck.rs", "Config"),
+             ("pow_config", "src/protocols/proof_of_work.rs", "Config"),
+             ("field_info", "src/algebra/fields.rs", "FieldInfo"),
+             ("identity", "src/algebra/embedding.rs", "Identity"),
+             ("basefield", "src/algebra/embedding.rs", "Basefield"),
+             ("typed_value", "src/type_info.rs", "TypedValue")]
+    out = {}
+    for key, rel, name in specs:
+        fields, line = struct_fields(read(root, rel), name)
+        out[key] = {"fields": fields, "at": "%s:%d" % (rel, line)}
+    emb = read(root, "src/algebra/embedding.rs")
+    for e in ("Identity", "Basefield"):
+        s, line = type_info_string(emb, e)
+        out[e.lower() + "_type_info"] = {"value": s, "at": "src/algebra/embedding.rs:%d" % line}
+    return out
+
+
 def main(root):
     out = {"source": "WizardOfMenlo/whir reference sources"}
     b3 = read(root, "src/hash/blake3_engine.rs")
@@ -105,6 +170,7 @@ def main(root):
     fl = "\n".join(read(root, "src/algebra/fields.rs"))
     m = re.search(r'"\{\\"characteristic\\":\\"([0-9a-f]+)\\",\\"extension_degree\\":(\d+)\}"', fl)
     out["field_type_info_goldilocks3"] = {"characteristic": m.group(1), "extension_degree": int(m.group(2))}
+    out["serde_config_layout"] = serde_layout(root)
     tw = "\n".join(read(root, "src/algebra/ntt/cooley_tukey.rs"))
     assert "assert_eq!(values[4], Field64::from(5) * roots[10]);" in tw
     return out

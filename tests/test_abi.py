@@ -68,14 +68,15 @@ def test_config_matches_oracle(orc):
 
 
 def test_config_bytes_match_oracle(orc):
-    # The protocol id hashes identical configuration bytes in both implementations: a GPU transcript
-    # and an oracle transcript with the same session start from the same sponge state. Checked
-    # indirectly: an empty prover state must agree with the oracle's first squeeze.
+    # The protocol id hashes identical configuration bytes in both implementations (the CBOR of the
+    # configuration, a map of six entries), so a GPU transcript and an oracle transcript with the same
+    # session start from the same sponge state.
     p = W.ProtocolParameters(unique_decoding=True, security_level=100, pow_bits=20)
     c = W.Config("Goldilocks2", 1 << 12, p)
     ob = orc.whir_config_bytes(orc.GOLDILOCKS2, orc.make_params(unique_decoding=True, security_level=100,
                                                                 pow_bits=20), 12)
-    assert ob.startswith(b"whir-gb300 config v1")
+    assert ob == c.cbor()
+    assert ob[:1] == b"\xa6" and ob[1:19] == b"\x71initial_committer"
 
 
 def test_no_device_fails_loudly():

@@ -296,6 +296,15 @@ class Config:
         _check(load_library().whir_config_json(self._h, buf, ctypes.c_size_t(1 << 16)))
         return json.loads(buf.value.decode())
 
+    def cbor(self):
+        """CBOR of the configuration's serde form (ciborium::into_writer): the protocol-id preimage."""
+        lib = load_library()
+        n = ctypes.c_size_t()
+        _check(lib.whir_config_cbor(self._h, None, ctypes.c_size_t(0), ctypes.byref(n)))
+        buf = (ctypes.c_uint8 * max(n.value, 1))()
+        _check(lib.whir_config_cbor(self._h, buf, ctypes.c_size_t(n.value), ctypes.byref(n)))
+        return bytes(buf[: n.value])
+
     def commit(self, ctx, prover_state, vectors, on_device=False):
         """vectors: batch_size x size source elements (numpy uint64), or a device pointer (int) with
         on_device=True."""

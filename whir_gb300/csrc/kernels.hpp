@@ -200,6 +200,53 @@ cudaError_t launch_mle_dot(const S* x, size_t n, const T* tables, int nv, T* par
 template <class T>
 cudaError_t launch_eq_table(const T* point, int off, int cnt, T scalar, T* table, cudaStream_t s);
 
+// Initial sumcheck over a = sum_j c_j lift(x_j) and a covector that is a sum of tensor-product
+// forms (eq forms of evaluation points, geometric forms of out-of-domain points): one pass over the
+// vectors gives the 2^k sums from which the host derives all k round messages (launch_tensor_sums),
+// a second pass after the last challenge writes the folded a and b (launch_tensor_fold). The
+// tables hold, per form, the tensor weights of variables k..n-1 split into rows then columns
+// (built by launch_tensor_table from per-variable (alpha, beta) pairs).
+static constexpr int TS_THREADS = 256;
+static constexpr int TS_MAX_FORMS = 4;
+static constexpr int TS_MAX_RPC = 32;  // rows per CTA in the sums pass
+
+struct TensorShape {
+  int k, R, C;         // folded variables, row bits, column bits (n = k + R + C)
+  int nvec, nforms;    // vectors (RLC'd) and tensor forms
+  uint64_t vec_stride;  // elements between consecutive vectors
+  int rpc;             // rows per CTA (sums pass)
+  int threads;         // CTA threads (sums pass; a multiple of 32)
+  uint64_t col_tiles, row_groups;
+  uint64_t grid() const { return ((uint64_t)nvec << k) * row_groups * col_tiles; }
+};
+
+inline TensorShape tensor_plan(int nvars, int k, int nvec, int nforms, uint64_t vec_stride) {
+  TensorShape sh;
+  sh.k = k;
+  const int rest = nvars - k;
+  sh.R = std::min(rest, std::max(4, rest - 12));
+  sh.C = rest - sh.R;
+  sh.nvec = nvec;
+  sh.nforms = nforms;
+  sh.vec_stride = vec_stride;
+  sh.rpc = (int)std::min<uint64_t>(1ull << sh.R, TS_MAX_RPC);
+  const uint64_t cols = 1ull << sh.C;
+  sh.threads = (int)std::max<uint64_t>(32, std::min<uint64_t>(TS_THREADS, cols));
+  sh.col_tiles = (cols + sh.threads - 1) / sh.threads;
+  sh.row_groups = (1ull << sh.R) / sh.rpc;
+  return sh;
+}
+
+template <class T, class S>
+cudaError_t launch_tensor_sums(const S* x, const TensorShape& sh, const T* tables, T* partials, T* out,
+                               unsigned int* counter, cudaStream_t s);
+template <class T, class S>
+cudaError_t launch_tensor_fold(const S* x, const TensorShape& sh, const T* w, const T* kf, const T* tables, T* a_out,
+                               T* b_out, cudaStream_t s);
+// out[e] = scalar * prod_q (bit_{cnt-1-q}(e) ? ab[2q+1] : ab[2q]) for e < 2^cnt (device arrays).
+template <class T>
+cudaError_t launch_tensor_table(const T* ab, int cnt, T scalar, T* out, cudaStream_t s);
+
 // dst[i] = map(v0[i]) + sum_{j>=1} coeffs[j] * v_j[i]  (lift + mixed_scalar_mul_add, algebra/mod.rs:51-98)
 template <class T, class S>
 cudaError_t launch_lift_rlc(T* dst, const S* const* vecs, const T* coeffs, size_t nvec, size_t n, cudaStream_t s);

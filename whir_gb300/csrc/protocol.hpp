@@ -471,7 +471,8 @@ inline Config config_new(int field, size_t size, const Params& wp) {
   return cfg;
 }
 
-// Canonical configuration bytes hashed into the protocol id (SHA3-512).
+// CBOR of the configuration (ciborium::into_writer of whir::Config), hashed into the protocol id
+// (SHA3-512).
 inline std::vector<uint8_t> config_bytes(const Config& c);
 
 }  // namespace whir
@@ -483,55 +484,238 @@ struct whir_config {
 
 namespace whir {
 
-inline std::vector<uint8_t> config_bytes(const Config& c) {
-  std::vector<uint8_t> o;
-  auto u64 = [&](uint64_t v) {
-    for (int i = 0; i < 8; ++i) o.push_back((uint8_t)(v >> (8 * i)));
-  };
-  auto bytes = [&](const uint8_t* b, size_t n) { o.insert(o.end(), b, b + n); };
-  auto irs = [&](const Irs& r) {
-    u64(r.num_vectors);
-    u64(r.vector_size);
-    u64(r.mask_length);
-    u64(r.codeword_length);
-    u64(r.interleaving_depth);
-    u64(r.num_cols);
-    bytes(r.hash_id, 32);
-    u64(r.codeword_length);
-    u64(r.layers);
-    bytes(r.hash_id, 32);
-    uint64_t js;
-    memcpy(&js, &r.johnson_slack, 8);
-    u64(js);
-    u64(r.in_domain_samples);
-    u64(r.out_domain_samples);
-    u64(r.dedup ? 1 : 0);
-  };
-  auto pow = [&](const Pow& p) {
-    bytes(p.hash_id, 32);
-    u64(p.threshold);
-  };
-  auto sc = [&](const Sumcheck& s) {
-    u64(s.initial_size);
-    pow(s.round_pow);
-    u64(s.num_rounds);
-    u64(s.mask_length);
-  };
-  const char* tag = "whir-gb300 config v1";
-  bytes(reinterpret_cast<const uint8_t*>(tag), strlen(tag));
-  u64((uint64_t)c.field);
-  irs(c.initial);
-  sc(c.initial_sumcheck);
-  pow(c.initial_skip_pow);
-  u64(c.rounds.size());
-  for (auto& r : c.rounds) {
-    irs(r.irs);
-    sc(r.sumcheck);
-    pow(r.pow);
+// CBOR (RFC 8949) writer with the encoding choices ciborium 0.2 makes for serde data: integers,
+// lengths and tags in their shortest head; definite-length arrays, maps, byte and text strings;
+// floats in the shortest of binary16 / binary32 / binary64 that keeps the value's exact bits.
+struct CborWriter {
+  std::vector<uint8_t> out;
+  void head(unsigned major, uint64_t v) {
+    const uint8_t m = (uint8_t)(major << 5);
+    if (v < 24) {
+      out.push_back(m | (uint8_t)v);
+    } else if (v <= 0xff) {
+      out.push_back(m | 24);
+      out.push_back((uint8_t)v);
+    } else if (v <= 0xffff) {
+      out.push_back(m | 25);
+      be(v, 2);
+    } else if (v <= 0xffffffffull) {
+      out.push_back(m | 26);
+      be(v, 4);
+    } else {
+      out.push_back(m | 27);
+      be(v, 8);
+    }
   }
-  sc(c.final_sumcheck);
-  pow(c.final_pow);
-  return o;
+  void be(uint64_t v, int bytes) {
+    for (int i = bytes - 1; i >= 0; --i) out.push_back((uint8_t)(v >> (8 * i)));
+  }
+  void uint(uint64_t v) { head(0, v); }
+  void bytes(const uint8_t* b, size_t n) {
+    head(2, n);
+    out.insert(out.end(), b, b + n);
+  }
+  void text(const char* s) {
+    const size_t n = strlen(s);
+    head(3, n);
+    out.insert(out.end(), s, s + n);
+  }
+  void array(size_t n) { head(4, n); }
+  void map(size_t n) { head(5, n); }
+  void boolean(bool b) { out.push_back(b ? 0xf5 : 0xf4); }
+  // binary16 bits of d when d converts to binary16 exactly (finite values only).
+  static bool to_half(double d, uint16_t* h) {
+    if (!std::isfinite(d)) return false;
+    const uint16_t sign = std::signbit(d) ? 0x8000 : 0;
+    const double a = std::fabs(d);
+    if (a == 0.0) {
+      *h = sign;
+      return true;
+    }
+    int e;
+    const double m = std::frexp(a, &e);  // a = m * 2^e, m in [0.5, 1)
+    // normal binary16: a = (1 + f / 1024) * 2^(E - 15), E in [1, 30]  <=>  e - 1 = E - 15
+    const int E = e - 1 + 15;
+    if (E >= 1 && E <= 30) {
+      const double f = (m * 2.0 - 1.0) * 1024.0;
+      if (f != std::floor(f)) return false;
+      *h = (uint16_t)(sign | (E << 10) | (uint16_t)f);
+      return true;
+    }
+    if (E < 1) {  // subnormal: a = f * 2^-24, f in [1, 1023]
+      const double f = std::ldexp(a, 24);
+      if (f != std::floor(f) || f < 1.0 || f > 1023.0) return false;
+      *h = (uint16_t)(sign | (uint16_t)f);
+      return true;
+    }
+    return false;
+  }
+  void f64(double d) {
+    uint16_t h;
+    if (to_half(d, &h)) {
+      out.push_back(0xf9);
+      be(h, 2);
+      return;
+    }
+    const float f = (float)d;
+    if (std::isfinite(d) && (double)f == d) {
+      uint32_t b;
+      memcpy(&b, &f, 4);
+      out.push_back(0xfa);
+      be(b, 4);
+      return;
+    }
+    uint64_t b;
+    memcpy(&b, &d, 8);
+    out.push_back(0xfb);
+    be(b, 8);
+  }
+};
+
+// The serde data model of whir::Config<M> (protocols/whir/mod.rs:29-46) as ciborium::into_writer
+// writes it for the protocol id (transcript/mod.rs:111-121): structs are maps keyed by their field
+// names in declaration order; EngineId ([u8; 32] newtype) is an array of 32 integers; usize and u64
+// are unsigned integers; OrderedFloat<f64> is a float; Typed<M> is {"type": M's type info, "value":
+// M} (type_info.rs:98-117); a field's type info is FieldInfo {characteristic: big-endian bytes
+// without leading zeros, extension_degree} (fields.rs:32-62); embeddings serialize their one Type
+// field ("field" for Identity, "extension" for Basefield, embedding.rs:43-59, 191-205).
+inline void cbor_field_info(CborWriter& w, int base_field, size_t degree) {
+  std::vector<uint8_t> le;
+  if (base_field == 4 || base_field == 5) {
+    const int n = base_field == 4 ? F192Params::N : F256Params::N;
+    for (int i = 0; i < n; ++i) {
+      const uint64_t limb = base_field == 4 ? F192Params::p(i) : F256Params::p(i);
+      for (int b = 0; b < 8; ++b) le.push_back((uint8_t)(limb >> (8 * b)));
+    }
+  } else {
+    for (int b = 0; b < 8; ++b) le.push_back((uint8_t)(GL_P >> (8 * b)));
+  }
+  while (!le.empty() && le.back() == 0) le.pop_back();
+  std::vector<uint8_t> bev(le.rbegin(), le.rend());
+  w.map(2);
+  w.text("characteristic");
+  w.bytes(bev.data(), bev.size());
+  w.text("extension_degree");
+  w.uint(degree);
+}
+// Base prime field and extension degree of an embedding id's target field.
+inline void field_parts(int field, int* base, size_t* degree) {
+  if (field >= 0 && field <= 2) {
+    *base = 0;
+    *degree = (size_t)field + 1;
+  } else {
+    *base = field;
+    *degree = 1;
+  }
+}
+inline void cbor_engine(CborWriter& w, const uint8_t* id) {
+  w.array(32);
+  for (int i = 0; i < 32; ++i) w.uint(id[i]);
+}
+inline void cbor_pow(CborWriter& w, const Pow& p) {
+  w.map(2);
+  w.text("hash_id");
+  cbor_engine(w, p.hash_id);
+  w.text("threshold");
+  w.uint(p.threshold);
+}
+inline void cbor_sumcheck(CborWriter& w, const Sumcheck& s, int field) {
+  int base;
+  size_t degree;
+  field_parts(field, &base, &degree);
+  w.map(5);
+  w.text("field");
+  cbor_field_info(w, base, degree);
+  w.text("initial_size");
+  w.uint(s.initial_size);
+  w.text("round_pow");
+  cbor_pow(w, s.round_pow);
+  w.text("num_rounds");
+  w.uint(s.num_rounds);
+  w.text("mask_length");
+  w.uint(s.mask_length);
+}
+// irs_commit::Config<M> (irs_commit.rs:51-91) for the embedding `field` (basefield: the initial
+// committer of an extension-field config), or the identity embedding of the target field (rounds).
+inline void cbor_irs(CborWriter& w, const Irs& r, int field, bool identity) {
+  int base;
+  size_t degree;
+  field_parts(field, &base, &degree);
+  const bool basefield = !identity && degree > 1;
+  w.map(11);
+  w.text("embedding");
+  w.map(2);
+  w.text("type");
+  w.text(basefield ? "basefield" : "identity");
+  w.text("value");
+  w.map(1);
+  w.text(basefield ? "extension" : "field");
+  cbor_field_info(w, base, degree);
+  w.text("num_vectors");
+  w.uint(r.num_vectors);
+  w.text("vector_size");
+  w.uint(r.vector_size);
+  w.text("mask_length");
+  w.uint(r.mask_length);
+  w.text("codeword_length");
+  w.uint(r.codeword_length);
+  w.text("interleaving_depth");
+  w.uint(r.interleaving_depth);
+  w.text("matrix_commit");  // matrix_commit::Config (matrix_commit.rs:93-111), with_hash
+  w.map(4);
+  w.text("element_type");
+  cbor_field_info(w, base, basefield ? 1 : degree);
+  w.text("num_cols");
+  w.uint(r.num_cols);
+  w.text("leaf_hash_id");
+  cbor_engine(w, r.hash_id);
+  w.text("merkle_tree");  // merkle_tree::Config (merkle_tree.rs:25-40)
+  w.map(2);
+  w.text("num_leaves");
+  w.uint(r.codeword_length);
+  w.text("layers");
+  w.array(r.layers);
+  for (size_t l = 0; l < r.layers; ++l) {
+    w.map(1);
+    w.text("hash_id");
+    cbor_engine(w, r.hash_id);
+  }
+  w.text("johnson_slack");
+  w.f64(r.johnson_slack);
+  w.text("in_domain_samples");
+  w.uint(r.in_domain_samples);
+  w.text("out_domain_samples");
+  w.uint(r.out_domain_samples);
+  w.text("deduplicate_in_domain");
+  w.boolean(r.dedup);
+}
+
+// CBOR of the configuration: the bytes whose SHA3-512 is the protocol id.
+inline std::vector<uint8_t> config_bytes(const Config& c) {
+  CborWriter w;
+  w.map(6);
+  w.text("initial_committer");
+  cbor_irs(w, c.initial, c.field, false);
+  w.text("initial_sumcheck");
+  cbor_sumcheck(w, c.initial_sumcheck, c.field);
+  w.text("initial_skip_pow");
+  cbor_pow(w, c.initial_skip_pow);
+  w.text("round_configs");
+  w.array(c.rounds.size());
+  for (const Round& r : c.rounds) {
+    w.map(3);
+    w.text("irs_committer");
+    cbor_irs(w, r.irs, c.field, true);
+    w.text("sumcheck");
+    cbor_sumcheck(w, r.sumcheck, c.field);
+    w.text("pow");
+    cbor_pow(w, r.pow);
+  }
+  w.text("final_sumcheck");
+  cbor_sumcheck(w, c.final_sumcheck, c.field);
+  w.text("final_pow");
+  cbor_pow(w, c.final_pow);
+  return w.out;
 }
 
 // Sibling digests a Merkle opening must reveal, in the order merkle_tree.rs:145-186 writes them;

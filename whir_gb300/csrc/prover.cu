@@ -922,6 +922,113 @@ std::vector<T> initial_sumcheck_fused(whir_ctx* ctx, const Sumcheck& c, Transcri
   return rs;
 }
 
+// One tensor-product form of the initial covector: B(y) = scalar * prod_t (y_t ? beta[t] : alpha[t])
+// over the index bits y_t, t = 0 the most significant (an eq form of an evaluation point p has
+// (alpha, beta) = (1 - p_t, p_t); the geometric form of an out-of-domain point x has
+// (1, x^(2^(n-1-t)))).
+template <class T>
+struct TensorForm {
+  T scalar;
+  std::vector<T> alpha, beta;
+};
+
+// Initial sumcheck (protocols/sumcheck.rs:69-162, mask_length == 0) over a = x_0 + sum_{j>=1}
+// c_j lift(x_j) (the vector RLC, as lift + mixed_scalar_mul_add) and b = sum_f B_f for tensor
+// forms B_f. The device makes one pass over the vectors for the 2^k sums V_{j,f}(z) (launch_tensor_sums);
+// the host derives every round message from them: with the earlier challenges folded into V and
+// into P_f = prod_{u<t} phi_{f,u}(r_u), round t's polynomial is
+//   h_t(X) = sum_{j,f} c_j s_f P_f phi_{f,t}(X) (A_{j,f,0} + X (A_{j,f,1} - A_{j,f,0})),
+//   A_{j,f,c} = sum_y V_{j,f}(c, y) prod_{u>t} phi_{f,u}(y_u),
+// which gives the reference's (c0, c2) exactly (c0 = h_t(0), c2 its X^2 coefficient). After the last
+// challenge one more pass writes the folded a and b (launch_tensor_fold). The transcript
+// interactions (messages, round PoW, challenges) are those of sumcheck_device.
+template <class T, class S>
+std::vector<T> initial_sumcheck_tensor(whir_ctx* ctx, const Sumcheck& c, Transcript& ts, const S* x, size_t nvec,
+                                       const std::vector<T>& vector_rlc, const std::vector<TensorForm<T>>& forms,
+                                       T* a, T* b, size_t& n, T& sum) {
+  const int nvars = (int)layers_for(n);
+  const int k = (int)c.num_rounds;
+  const int NF = (int)forms.size();
+  const TensorShape sh = tensor_plan(nvars, k, (int)nvec, NF, n);
+  const size_t rows = (size_t)1 << sh.R, cols = (size_t)1 << sh.C, per = rows + cols;
+  const size_t nz = (size_t)1 << k;
+  std::vector<T> rs;
+  DBuf<T> tables(ctx, NF * per), parts(ctx, sh.grid() * NF), out(ctx, nvec * NF * nz);
+  std::vector<T> V(nvec * NF * nz);
+  {
+    ProfScope prof(ctx, PF_SUMCHECK);
+    std::vector<T> ab;
+    for (const auto& f : forms)
+      for (int t = k; t < nvars; ++t) {
+        ab.push_back(f.alpha[t]);
+        ab.push_back(f.beta[t]);
+      }
+    DBuf<T> dab(ctx, std::max<size_t>(ab.size(), 1));
+    h2d(ctx, dab.p, ab.data(), ab.size() * sizeof(T));
+    const size_t pf = 2 * (size_t)(nvars - k);
+    for (int f = 0; f < NF; ++f) {
+      CU(launch_tensor_table<T>(dab.p + f * pf, sh.R, T::one(), tables.p + f * per, ctx->stream));
+      CU(launch_tensor_table<T>(dab.p + f * pf + 2 * sh.R, sh.C, T::one(), tables.p + f * per + rows, ctx->stream));
+    }
+    CU((launch_tensor_sums<T, S>(x, sh, tables.p, parts.p, out.p, ctx->sc_counter, ctx->stream)));
+    d2h(ctx, V.data(), out.p, V.size() * sizeof(T));
+  }
+  std::vector<T> P(NF, T::one());
+  for (int t = 0; t < k; ++t) {
+    const size_t sz = nz >> t, half = sz >> 1;
+    T c0 = T::zero(), c2 = T::zero();
+    for (int f = 0; f < NF; ++f) {
+      const TensorForm<T>& fm = forms[f];
+      // weights of the remaining top variables t+1..k-1 inside a half
+      std::vector<T> wy(half, T::one());
+      for (size_t y = 0; y < half; ++y)
+        for (int q = 0; q < k - t - 1; ++q) {
+          const bool bit = (y >> (k - t - 2 - q)) & 1;
+          wy[y] = wy[y] * (bit ? fm.beta[t + 1 + q] : fm.alpha[t + 1 + q]);
+        }
+      for (size_t j = 0; j < nvec; ++j) {
+        const T* v = &V[(j * NF + f) * nz];
+        T A0 = T::zero(), A1 = T::zero();
+        for (size_t y = 0; y < half; ++y) {
+          A0 += v[y] * wy[y];
+          A1 += v[half + y] * wy[y];
+        }
+        const T coef = (j == 0 ? T::one() : vector_rlc[j]) * fm.scalar * P[f];
+        c0 += coef * (fm.alpha[t] * A0);
+        c2 += coef * ((fm.beta[t] - fm.alpha[t]) * (A1 - A0));
+      }
+    }
+    const T c1 = sum - c0.dbl() - c2;
+    send_elem<T>(ts, c0);
+    send_elem<T>(ts, c2);
+    pow_prove(ctx, c.round_pow, ts);
+    const T r = challenge<T>(ts);
+    rs.push_back(r);
+    sum = (c2 * r + c1) * r + c0;
+    for (size_t jf = 0; jf < nvec * (size_t)NF; ++jf) {
+      T* v = &V[jf * nz];
+      for (size_t y = 0; y < half; ++y) v[y] = v[y] + r * (v[half + y] - v[y]);
+    }
+    for (int f = 0; f < NF; ++f) P[f] = P[f] * (forms[f].alpha[t] + r * (forms[f].beta[t] - forms[f].alpha[t]));
+  }
+  {
+    ProfScope prof(ctx, PF_SUMCHECK);
+    std::vector<T> w(nvec * nz), kf(NF);
+    for (size_t z = 0; z < nz; ++z) {
+      T e = T::one();
+      for (int t = 0; t < k; ++t) e = e * (((z >> (k - 1 - t)) & 1) ? rs[t] : T::one() - rs[t]);
+      for (size_t j = 0; j < nvec; ++j) w[j * nz + z] = (j == 0 ? T::one() : vector_rlc[j]) * e;
+    }
+    for (int f = 0; f < NF; ++f) kf[f] = forms[f].scalar * P[f];
+    DBuf<T> dw(ctx, w.size()), dk(ctx, kf.size());
+    h2d(ctx, dw.p, w.data(), w.size() * sizeof(T));
+    h2d(ctx, dk.p, kf.data(), kf.size() * sizeof(T));
+    CU((launch_tensor_fold<T, S>(x, sh, dw.p, dk.p, tables.p, a, b, ctx->stream)));
+  }
+  n >>= k;
+  return rs;
+}
+
 // covector[i] += sum_j scalars[j] * w_N^(exps[j] * i) for i < len: the STIR constraints of the
 // in-domain query points (UnivariateEvaluation::accumulate_many, linear_form/univariate_evaluation.rs
 // 26-39). Small rounds use the root-table kernel; when len * queries exceeds the cost of one size-N
@@ -1081,13 +1188,22 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
   const bool has_constraints = !constraint_rlc.empty();
   std::vector<T> init_rlc(constraint_rlc.begin(), constraint_rlc.begin() + nforms);
   std::vector<T> oods_rlc(constraint_rlc.begin() + nforms, constraint_rlc.end());
+  // Tensor path: the covector is a sum of at most TS_MAX_FORMS tensor-product forms (evaluation
+  // points and out-of-domain points; explicit covectors are not tensors) and the initial sumcheck
+  // has rounds: the vectors are read twice in all (initial_sumcheck_tensor).
+  const int nvars_all = (int)layers_for(n);
+  const size_t k0 = cfg.initial_sumcheck.num_rounds;
+  const bool tensor = has_constraints && covectors.empty() && mle_points.size() + oods_points.size() <= TS_MAX_FORMS &&
+                      k0 >= 1 && k0 <= 10 && (int)k0 <= nvars_all && cfg.initial_sumcheck.mask_length == 0 &&
+                      n == ((size_t)1 << nvars_all) && (nv << k0) * sizeof(T) <= 48 * 1024;
   // Fused path: one vector and a statement made only of multilinear-evaluation forms. The first
   // two sumcheck rounds then read the coefficients directly and evaluate the eq covector from
   // small tables, so neither the lifted vector nor the covector is written at full size.
-  const bool fused = has_constraints && nv == 1 && covectors.empty() && oods_points.empty() && !mle_points.empty() &&
-                     n >= 8 && cfg.initial_sumcheck.num_rounds >= 1;
-  DBuf<T> a(ctx, fused ? n / 2 : n), b(ctx, fused ? n / 2 : n);
-  if (!fused) {
+  const bool fused = !tensor && has_constraints && nv == 1 && covectors.empty() && oods_points.empty() &&
+                     !mle_points.empty() && n >= 8 && cfg.initial_sumcheck.num_rounds >= 1;
+  const size_t alen = tensor ? n >> k0 : (fused ? n / 2 : n);
+  DBuf<T> a(ctx, alen), b(ctx, alen);
+  if (!fused && !tensor) {
     std::vector<const S*> vp(nv);
     for (size_t j = 0; j < nv; ++j) vp[j] = d_vectors + j * n;
     ProfScope prof(ctx, PF_LIFT);
@@ -1108,7 +1224,7 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
       CU(launch_eq_table<T>(pt.p + k * nvars, 0, h, init_rlc[k], eq_tables.p + k * per, ctx->stream));
       CU(launch_eq_table<T>(pt.p + k * nvars, h, l, T::one(), eq_tables.p + k * per + (1ull << h), ctx->stream));
     }
-  } else if (has_constraints) {
+  } else if (has_constraints && !tensor) {
     CU(cudaMemsetAsync(b.p, 0, n * sizeof(T), ctx->stream));
     const int nvars = (int)layers_for(n);
     DBuf<T> pt(ctx, std::max(nvars, 1));
@@ -1141,7 +1257,7 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
     for (size_t j = 0; j < nv; ++j) row += vector_rlc[j] * evaluations[f * nv + j];
     the_sum += init_rlc[f] * row;
   }
-  if (!oods_points.empty()) {
+  if (!oods_points.empty() && !tensor) {
     DBuf<T> sp(ctx, 2 * oods_points.size());
     std::vector<T> packed(oods_rlc);
     packed.insert(packed.end(), oods_points.begin(), oods_points.end());
@@ -1157,7 +1273,28 @@ void prove_device(whir_ctx* ctx, const Config& cfg, Transcript& ts, const S* d_v
 
   size_t len = n;  // current logical length of a and b
   std::vector<T> folding;
-  if (fused) {
+  if (tensor) {
+    std::vector<TensorForm<T>> forms;
+    for (size_t f = 0; f < mle_points.size(); ++f) {
+      TensorForm<T> fm{init_rlc[f], {}, {}};
+      for (const T& p : mle_points[f]) {
+        fm.alpha.push_back(T::one() - p);
+        fm.beta.push_back(p);
+      }
+      forms.push_back(std::move(fm));
+    }
+    for (size_t o = 0; o < oods_points.size(); ++o) {
+      TensorForm<T> fm{oods_rlc[o], std::vector<T>(nvars_all, T::one()), std::vector<T>(nvars_all)};
+      T pw = oods_points[o];
+      for (int t = nvars_all - 1; t >= 0; --t) {
+        fm.beta[t] = pw;
+        pw = pw * pw;
+      }
+      forms.push_back(std::move(fm));
+    }
+    folding = initial_sumcheck_tensor<T, S>(ctx, cfg.initial_sumcheck, ts, d_vectors, nv, vector_rlc, forms, a.p, b.p,
+                                            len, the_sum);
+  } else if (fused) {
     folding = initial_sumcheck_fused<T, S>(ctx, cfg.initial_sumcheck, ts, d_vectors, eq_tables.p,
                                            (int)mle_points.size(), a.p, b.p, len, the_sum);
   } else if (has_constraints) {
@@ -1580,6 +1717,17 @@ int whir_config_json(const whir_config* cfg, char* buf, size_t cap) {
     s += tmp;
     if (!buf || s.size() + 1 > cap) throw Error(WHIR_ERR_INVALID, "buffer too small");
     memcpy(buf, s.c_str(), s.size() + 1);
+    return 0;
+  });
+}
+
+int whir_config_cbor(const whir_config* cfg, uint8_t* buf, size_t cap, size_t* len) {
+  return guarded([&] {
+    if (!cfg || !len) throw Error(WHIR_ERR_INVALID, "null argument");
+    const std::vector<uint8_t> cb = config_bytes(cfg->cfg);
+    *len = cb.size();
+    if (buf && cap) memcpy(buf, cb.data(), std::min(cap, cb.size()));
+    if (buf && cap < cb.size()) throw Error(WHIR_ERR_INVALID, "buffer too small for the configuration's CBOR");
     return 0;
   });
 }

@@ -883,6 +883,180 @@ cudaError_t launch_rows_finish(T* a, size_t m, T r, const T* F, int rlog, const 
 }
 
 // ---------------------------------------------------------------------------------------------
+// Initial sumcheck over covectors that are sums of tensor products (reference
+// protocols/sumcheck.rs:69-162 with a = sum_j c_j lift(x_j) and b = sum_f s_f B_f, where every form
+// is B_f(y) = prod_t phi_{f,t}(y_t) with phi(0) = alpha_t, phi(1) = beta_t: an eq form
+// eq(p, .) has (alpha, beta) = (1 - p_t, p_t), an out-of-domain geometric form x^i has
+// (1, x^(2^(n-1-t))); variable t = 0 is the most significant index bit).
+//
+// Round t's polynomial depends on the data only through the 2^k sums
+//   V_{j,f}(z) = sum_rest x_j(z, rest) * prod_{t >= k} phi_{f,t}(rest)      (z = top k index bits)
+// (the k folded variables enter through the challenges, the rest through the tensor weights), so
+// one pass over the vectors yields every round message of the k rounds, and a second pass after
+// the last challenge writes the folded vector a'(rest) = sum_{j,z} c_j eq(r, z) x_j(z, rest) and the
+// folded covector b'(rest) = sum_f K_f prod_{t >= k} phi_{f,t}(rest). The rest index is split into
+// 2^R rows and 2^C columns; per form, `tables` holds the row weights (2^R) then the column weights
+// (2^C) of the tensor over variables k.. n-1.
+// ---------------------------------------------------------------------------------------------
+// Sums pass. CTA (j, z, row group g, column tile): thread = one column, rows [g rpc, (g+1) rpc) of
+// the z block; per form the thread accumulates sum_rows row_w[H] x(H, col) unreduced, then
+// multiplies by its column weight; the CTA's per-form sums go to partials, and the last CTA adds the
+// partials of every (j, f, z) into out[(j nforms + f) 2^k + z].
+template <class T, class S, int NF>
+__global__ void __launch_bounds__(TS_THREADS) tensor_sums_kernel(const S* x, TensorShape sh, const T* tables,
+                                                                 T* partials, T* out, unsigned int* counter) {
+  __shared__ T srow[NF][TS_MAX_RPC];
+  __shared__ bool am_last;
+  const uint64_t rows = 1ull << sh.R, cols = 1ull << sh.C, per = rows + cols;
+  uint64_t bid = blockIdx.x;
+  const uint64_t tile = bid % sh.col_tiles;
+  bid /= sh.col_tiles;
+  const uint64_t g = bid % sh.row_groups;
+  bid /= sh.row_groups;
+  const uint64_t z = bid & ((1ull << sh.k) - 1), j = bid >> sh.k;
+  const uint64_t col = tile * blockDim.x + threadIdx.x;
+  const uint64_t r0 = g * sh.rpc;
+  for (int e = threadIdx.x; e < NF * sh.rpc; e += blockDim.x) {
+    const int f = e / sh.rpc, r = e - f * sh.rpc;
+    srow[f][r] = tables[(uint64_t)f * per + r0 + r];
+  }
+  __syncthreads();
+  WideAcc<T> acc[NF];
+#pragma unroll
+  for (int f = 0; f < NF; ++f) acc[f].init();
+  if (col < cols) {
+    const S* base = x + j * sh.vec_stride + ((z << sh.R) + r0) * cols + col;
+    int r = 0;
+    for (; r + 8 <= sh.rpc; r += 8) {
+      S v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = base[(uint64_t)(r + u) * cols];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int f = 0; f < NF; ++f) acc[f].mac_mixed(srow[f][r + u], v[u]);
+    }
+    for (; r < sh.rpc; ++r) {
+      const S v = base[(uint64_t)r * cols];
+#pragma unroll
+      for (int f = 0; f < NF; ++f) acc[f].mac_mixed(srow[f][r], v);
+    }
+  }
+  T mine[NF];
+#pragma unroll
+  for (int f = 0; f < NF; ++f) mine[f] = col < cols ? tables[(uint64_t)f * per + rows + col] * acc[f].get() : T::zero();
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    const T s = block_sum(mine[f]);
+    if (threadIdx.x == 0) partials[(uint64_t)blockIdx.x * NF + f] = s;
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    am_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  const uint64_t nz = 1ull << sh.k, groups = sh.row_groups * sh.col_tiles;
+  const uint64_t nout = (uint64_t)sh.nvec * NF * nz;
+  for (uint64_t o = threadIdx.x; o < nout; o += blockDim.x) {
+    const uint64_t zz = o % nz, f = (o / nz) % NF, jj = o / (nz * NF);
+    const T* p = partials + ((jj * nz + zz) * groups) * NF + f;
+    T s = T::zero();
+    for (uint64_t q = 0; q < groups; ++q) s += ldcg_t(p + q * NF);
+    out[o] = s;
+  }
+  if (threadIdx.x == 0) counter[0] = 0;
+}
+
+// Fold pass: a_out[i] = sum_{j, z} w[j 2^k + z] x_j(z, i) and b_out[i] = sum_f kf[f] row_f[i >> C]
+// col_f[i & (2^C - 1)] for i < 2^(R + C).
+template <class T, class S>
+__global__ void __launch_bounds__(TS_THREADS) tensor_fold_kernel(const S* x, TensorShape sh, const T* w,
+                                                                 const T* kf, const T* tables, T* a_out,
+                                                                 T* b_out) {
+  extern __shared__ unsigned char ts_smem[];
+  T* sw = reinterpret_cast<T*>(ts_smem);
+  const int nw = sh.nvec << sh.k;
+  for (int e = threadIdx.x; e < nw; e += blockDim.x) sw[e] = w[e];
+  __syncthreads();
+  const uint64_t rows = 1ull << sh.R, cols = 1ull << sh.C, per = rows + cols, len = rows * cols;
+  const uint64_t zstride = len, nz = 1ull << sh.k;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < len; i += (uint64_t)gridDim.x * blockDim.x) {
+    WideAcc<T> acc;
+    acc.init();
+    for (int j = 0; j < sh.nvec; ++j) {
+      const S* xj = x + (uint64_t)j * sh.vec_stride + i;
+      const T* wj = sw + ((uint64_t)j << sh.k);
+      uint64_t z = 0;
+      for (; z + 8 <= nz; z += 8) {
+        S v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = xj[(z + u) * zstride];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc.mac_mixed(wj[z + u], v[u]);
+      }
+      for (; z < nz; ++z) acc.mac_mixed(wj[z], xj[z * zstride]);
+    }
+    a_out[i] = acc.get();
+    const uint64_t H = i >> sh.C, c = i & (cols - 1);
+    T bv = T::zero();
+    for (int f = 0; f < sh.nforms; ++f) {
+      const T* tf = tables + (uint64_t)f * per;
+      bv += kf[f] * (tf[H] * tf[rows + c]);
+    }
+    b_out[i] = bv;
+  }
+}
+
+// Tensor table of `cnt` variables: out[e] = scalar * prod_q (bit_{cnt-1-q}(e) ? ab[2q+1] : ab[2q]).
+template <class T>
+__global__ void tensor_table_kernel(const T* ab, int cnt, T scalar, T* out) {
+  const uint64_t size = 1ull << cnt;
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < size; e += (uint64_t)gridDim.x * blockDim.x) {
+    T v = scalar;
+    for (int q = 0; q < cnt; ++q) v = v * ab[2 * q + ((e >> (cnt - 1 - q)) & 1)];
+    out[e] = v;
+  }
+}
+
+template <class T, class S>
+cudaError_t launch_tensor_sums(const S* x, const TensorShape& sh, const T* tables, T* partials, T* out,
+                               unsigned int* counter, cudaStream_t s) {
+  const unsigned grid = (unsigned)sh.grid();
+  switch (sh.nforms) {
+    case 1: tensor_sums_kernel<T, S, 1><<<grid, sh.threads, 0, s>>>(x, sh, tables, partials, out, counter); break;
+    case 2: tensor_sums_kernel<T, S, 2><<<grid, sh.threads, 0, s>>>(x, sh, tables, partials, out, counter); break;
+    case 3: tensor_sums_kernel<T, S, 3><<<grid, sh.threads, 0, s>>>(x, sh, tables, partials, out, counter); break;
+    case 4: tensor_sums_kernel<T, S, 4><<<grid, sh.threads, 0, s>>>(x, sh, tables, partials, out, counter); break;
+    default: return cudaErrorInvalidValue;
+  }
+  note_launch();
+  return cudaGetLastError();
+}
+
+template <class T, class S>
+cudaError_t launch_tensor_fold(const S* x, const TensorShape& sh, const T* w, const T* kf, const T* tables, T* a_out,
+                               T* b_out, cudaStream_t s) {
+  const uint64_t len = 1ull << (sh.R + sh.C);
+  const size_t smem = ((size_t)sh.nvec << sh.k) * sizeof(T);
+  if (smem > 48 * 1024) return cudaErrorInvalidValue;
+  const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((len + TS_THREADS - 1) / TS_THREADS,
+                                                                           SC_MAX_BLOCKS * 4));
+  tensor_fold_kernel<T, S><<<grid, TS_THREADS, smem, s>>>(x, sh, w, kf, tables, a_out, b_out);
+  note_launch();
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_tensor_table(const T* ab, int cnt, T scalar, T* out, cudaStream_t s) {
+  tensor_table_kernel<T><<<(unsigned)std::max<size_t>(1, ((1ull << cnt) + 255) / 256), 256, 0, s>>>(ab, cnt, scalar,
+                                                                                                   out);
+  note_launch();
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
 // Multilinear evaluation sum_i map(x_i) * eq(point, i) with the eq weights taken from one pair of
 // hi / lo tables (tables[0..2^h) and tables[2^h .. 2^h + 2^l)); block sums go to partials.
 // ---------------------------------------------------------------------------------------------
@@ -978,7 +1152,8 @@ cudaError_t launch_univariate_eval(const S* coeffs, size_t n, T x, T* partials, 
   template cudaError_t launch_scatter<T>(T*, const uint64_t*, const T*, size_t, cudaStream_t);                   \
   template cudaError_t launch_add<T>(T*, const T*, size_t, cudaStream_t);                                        \
   template cudaError_t launch_eq_table<T>(const T*, int, int, T, T*, cudaStream_t);                              \
-  template cudaError_t launch_rows_finish<T>(T*, size_t, T, const T*, int, const T*, int, int, T*, cudaStream_t);
+  template cudaError_t launch_rows_finish<T>(T*, size_t, T, const T*, int, const T*, int, int, T*, cudaStream_t);  \
+  template cudaError_t launch_tensor_table<T>(const T*, int, T, T*, cudaStream_t);
 
 // Kernels that read coefficient vectors over S and compute over T.
 #define WHIR_SC_EMBED_INST(T, S)                                                                                 \
@@ -990,6 +1165,10 @@ cudaError_t launch_univariate_eval(const S* coeffs, size_t n, T x, T* partials, 
   template cudaError_t launch_lift_rlc<T, S>(T*, const S* const*, const T*, size_t, size_t, cudaStream_t);       \
   template cudaError_t launch_univariate_eval<T, S>(const S*, size_t, T, T*, size_t*, cudaStream_t);             \
   template cudaError_t launch_rows_fold_compute<T, S>(const S*, size_t, T, const T*, size_t, int, const T*, int,  \
-                                                      int, T*, T*, T*, size_t*, cudaStream_t, T*, unsigned int*);
+                                                      int, T*, T*, T*, size_t*, cudaStream_t, T*, unsigned int*); \
+  template cudaError_t launch_tensor_sums<T, S>(const S*, const TensorShape&, const T*, T*, T*, unsigned int*,     \
+                                                cudaStream_t);                                                   \
+  template cudaError_t launch_tensor_fold<T, S>(const S*, const TensorShape&, const T*, const T*, const T*, T*, T*, \
+                                                cudaStream_t);
 
 }  // namespace whir
