@@ -120,6 +120,14 @@ int whir_prover_state_proof(const whir_prover_state* ps, const uint8_t** narg, s
  * witness (codeword matrix and Merkle nodes) stays resident on the device. */
 int whir_commit(whir_ctx* ctx, const whir_config* cfg, whir_prover_state* ps, const uint64_t* vectors,
                 uint32_t flags, whir_witness** out);
+/* Config::commit for n independent jobs at once: the batched form of whir_commit (the reference
+ * commits one job per call, irs_commit.rs:292-350). All jobs share one embedding and one hash
+ * engine; their sizes may differ. The device work of every job runs in shared launches (one encode
+ * column pass, one encode row pass with the leaf hashes, one Merkle launch per tile step, one
+ * fetch of all roots); then each job's transcript receives its root and out-of-domain samples
+ * exactly as whir_commit writes them. out[j] receives job j's witness (NULL on failure). */
+int whir_commit_batch(whir_ctx* ctx, size_t n, const whir_config* const* cfgs, whir_prover_state* const* pss,
+                      const uint64_t* const* vectors, uint32_t flags, whir_witness** out);
 int whir_witness_free(whir_witness* w);
 int whir_witness_root(const whir_witness* w, uint8_t root[32]);
 
@@ -150,6 +158,21 @@ int whir_verify(const whir_config* cfg, const char* session, size_t session_len,
                 const uint64_t* evaluations);
 /* Reason of the calling thread's last whir_verify rejection or error (no reference counterpart). */
 const char* whir_verify_last_reason(void);
+
+/* ---- autotuning (no reference counterpart: the reference has no device schedules) -------------
+ * whir_autotune times, on this context's device, every valid encode plan (whole cosets per CTA, or
+ * the four-step split's row-pass size and column-pass width) and Merkle tile height for the
+ * commitment shapes that Config::new derived for `cfg` (the initial commitment and every round's),
+ * and records the fastest in a process-wide table that later encodes and trees of those shapes use
+ * (results are bit-identical whatever the choice). report (nullable) receives a JSON summary of the
+ * candidates' milliseconds. The table is exported / imported as text lines
+ *   "encode <n_msgs> <msg_len> <codeword_len> <elem_bytes> <mode> <logC2> <W> <G>"
+ *   "merkle <layers> <tile_log>"
+ * so a serving process can load choices measured earlier; whir_autotune_clear empties it. */
+int whir_autotune(whir_ctx* ctx, const whir_config* cfg, int reps, char* report, size_t cap);
+int whir_autotune_export(char* buf, size_t cap, size_t* len);
+int whir_autotune_import(const char* text);
+int whir_autotune_clear(void);
 
 /* ---- operator-level entry points --------------------------------------------------------------- */
 /* ReedSolomon::interleaved_encode (src/algebra/ntt/mod.rs:89-99, cooley_tukey.rs:411-477) via

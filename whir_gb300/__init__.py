@@ -373,6 +373,59 @@ class Config:
             pass
 
 
+def commit_batch(ctx, configs, prover_states, vectors, on_device=False):
+    """Config.commit for several jobs in shared device launches (whir_commit_batch): configs,
+    prover_states and vectors (host numpy arrays, or device pointers with on_device=True) are
+    parallel lists; all configs share one embedding and one hash engine. Returns the witnesses."""
+    lib = load_library()
+    n = len(configs)
+    if not (len(prover_states) == len(vectors) == n):
+        raise WhirError(-1, "configs, prover_states and vectors must have the same length")
+    cfg_h = (ctypes.c_void_p * max(n, 1))(*[c._h.value for c in configs])
+    ps_h = (ctypes.c_void_p * max(n, 1))(*[s._h.value for s in prover_states])
+    keep = []
+    vp = (ctypes.POINTER(ctypes.c_uint64) * max(n, 1))()
+    for i, v in enumerate(vectors):
+        if on_device:
+            vp[i] = ctypes.cast(ctypes.c_void_p(int(v)), ctypes.POINTER(ctypes.c_uint64))
+        else:
+            a = _as_u64(v).reshape(-1)
+            keep.append(a)
+            vp[i] = _u64ptr(a)
+    out = (ctypes.c_void_p * max(n, 1))()
+    _check(lib.whir_commit_batch(ctx._h, ctypes.c_size_t(n), cfg_h, ps_h, vp,
+                                 ctypes.c_uint32(DEVICE_PTRS if on_device else 0), out))
+    return [Witness(ctypes.c_void_p(out[i]), ctx) for i in range(n)]
+
+
+def autotune(ctx, config, reps=3):
+    """Times every valid encode plan and Merkle tile height for the commitment shapes of `config` on
+    the context's device and records the fastest (whir_autotune); returns the JSON report."""
+    import json
+    buf = ctypes.create_string_buffer(1 << 20)
+    _check(load_library().whir_autotune(ctx._h, config._h, ctypes.c_int(reps), buf, ctypes.c_size_t(1 << 20)))
+    return json.loads(buf.value.decode())
+
+
+def autotune_export():
+    """The process-wide tuned choices as text lines (whir_autotune_export)."""
+    lib = load_library()
+    n = ctypes.c_size_t()
+    _check(lib.whir_autotune_export(None, ctypes.c_size_t(0), ctypes.byref(n)))
+    buf = ctypes.create_string_buffer(n.value + 1)
+    _check(lib.whir_autotune_export(buf, ctypes.c_size_t(n.value + 1), ctypes.byref(n)))
+    return buf.value.decode()
+
+
+def autotune_import(text):
+    """Loads tuned choices written by autotune_export (whir_autotune_import)."""
+    _check(load_library().whir_autotune_import(text.encode()))
+
+
+def autotune_clear():
+    _check(load_library().whir_autotune_clear())
+
+
 # ----------------------------------------------------------------------------------------------
 # Operator-level functions (host numpy in, host numpy out)
 # ----------------------------------------------------------------------------------------------

@@ -20,6 +20,7 @@
 #include "hash.cuh"
 #include "kernels.hpp"
 #include "roots.cuh"
+#include "status.hpp"
 
 namespace whir {
 
@@ -206,8 +207,7 @@ struct EncMinCtas {
 };
 
 template <class F, int KIND>
-__global__ void __launch_bounds__(ENC_THREADS, EncMinCtas<F>::value) encode_rows_kernel(EncArgs<F> a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void encode_rows_body(const EncArgs<F>& a, uint64_t bid, unsigned char* smem_raw) {
   F* s = reinterpret_cast<F*>(smem_raw);
   const int M = a.M;
   const int logn = a.mode == 0 ? a.logC : a.logC2;
@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(ENC_THREADS, EncMinCtas<F>::value) encode_rows
 
   uint64_t c_base = 0, k1 = 0;
   if (a.mode == 0) {
-    c_base = (uint64_t)blockIdx.x * a.G;
+    c_base = bid * a.G;
     #pragma unroll 4
     for (int idx = threadIdx.x; idx < nvec * n; idx += blockDim.x) {
       const int vec = idx >> logn, j = idx & (n - 1);
@@ -233,8 +233,8 @@ __global__ void __launch_bounds__(ENC_THREADS, EncMinCtas<F>::value) encode_rows
     }
   } else {
     const uint64_t C1 = 1ull << a.logC1;
-    c_base = blockIdx.x >> a.logC1;
-    k1 = blockIdx.x & (C1 - 1);
+    c_base = bid >> a.logC1;
+    k1 = bid & (C1 - 1);
     #pragma unroll 4
     for (int idx = threadIdx.x; idx < M * n; idx += blockDim.x) {
       const int m = idx >> logn, j2 = idx & (n - 1);
@@ -328,19 +328,52 @@ __global__ void __launch_bounds__(ENC_THREADS, EncMinCtas<F>::value) encode_rows
   }
 }
 
+template <class F, int KIND>
+__global__ void __launch_bounds__(ENC_THREADS, EncMinCtas<F>::value) encode_rows_kernel(EncArgs<F> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  encode_rows_body<F, KIND>(a, blockIdx.x, smem_raw);
+}
+
+// One encode pass over several jobs (independent codewords of possibly different shapes) in one
+// launch: job j owns CTAs [jobs[j].cta_begin, jobs[j + 1].cta_begin) of the grid.
+template <class F>
+struct EncJob {
+  EncArgs<F> args;
+  uint64_t cta_begin;
+};
+template <class F>
+__device__ __forceinline__ int enc_job_of(const EncJob<F>* jobs, int njobs, uint64_t bid) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].cta_begin <= bid)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+template <class F, int KIND>
+__global__ void __launch_bounds__(ENC_THREADS, EncMinCtas<F>::value) encode_rows_multi_kernel(const EncJob<F>* jobs,
+                                                                                             int njobs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int j = enc_job_of(jobs, njobs, blockIdx.x);
+  const EncArgs<F> a = jobs[j].args;
+  encode_rows_body<F, KIND>(a, blockIdx.x - jobs[j].cta_begin, smem_raw);
+}
+
 // Four-step pass 1: NTT_C1 over columns j2 of the (C1 x C2) view of each twisted message,
 // multiplied by w_C^(j2 k1); intermediate layout [m][c][k1][j2].
 template <class F>
-__global__ void __launch_bounds__(ENC_THREADS, EncMinCtas<F>::value) encode_cols_kernel(EncArgs<F> a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void encode_cols_body(const EncArgs<F>& a, uint64_t bid, unsigned char* smem_raw) {
   F* s = reinterpret_cast<F*>(smem_raw);
   const int logn = a.logC1, n = 1 << logn, W = a.W;
   typedef typename F::Base B;
   const B* tw = reinterpret_cast<const B*>(a.rt.ntt);  // read through L1 (keeps shared memory for data)
   const uint64_t C2 = 1ull << a.logC2, N = 1ull << a.logN;
   const uint64_t tiles = C2 / W;
-  const uint64_t tile = blockIdx.x % tiles;
-  const uint64_t mc = blockIdx.x / tiles;  // m * K + c
+  const uint64_t tile = bid % tiles;
+  const uint64_t mc = bid / tiles;  // m * K + c
   const uint64_t c = mc % a.K, m = mc / a.K;
   // With W dividing the block size every thread keeps one column w, and its successive elements
   // are js = ENC_THREADS / W rows apart: the coset twist w_N^(c j) and the four-step twiddle
@@ -394,6 +427,20 @@ __global__ void __launch_bounds__(ENC_THREADS, EncMinCtas<F>::value) encode_cols
       a.dst[((mc << a.logC1) + k1) * C2 + j2] = v;
     }
   }
+}
+
+template <class F>
+__global__ void __launch_bounds__(ENC_THREADS, EncMinCtas<F>::value) encode_cols_kernel(EncArgs<F> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  encode_cols_body<F>(a, blockIdx.x, smem_raw);
+}
+template <class F>
+__global__ void __launch_bounds__(ENC_THREADS, EncMinCtas<F>::value) encode_cols_multi_kernel(const EncJob<F>* jobs,
+                                                                                             int njobs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int j = enc_job_of(jobs, njobs, blockIdx.x);
+  const EncArgs<F> a = jobs[j].args;
+  encode_cols_body<F>(a, blockIdx.x - jobs[j].cta_begin, smem_raw);
 }
 
 // Raises a kernel's dynamic shared-memory limit once per device. Each caller instantiation owns its
@@ -508,6 +555,121 @@ cudaError_t launch_encode(const EncodePlan& p, const F* src, size_t n_msgs, size
   return dispatch_rows<F>(a, hash_kind, (unsigned)(a.K * C1), smem, s);
 }
 
+// Multi-job encode: the host image holds the column-pass table then (16-byte aligned) the row-pass
+// table, one EncJob per job with the CTA index its range starts at.
+template <class F>
+size_t encode_multi_table_bytes(size_t njobs) {
+  return 2 * njobs * sizeof(EncJob<F>) + 64;
+}
+
+template <class F>
+static EncArgs<F> enc_args_of(const EncodeJobDesc& d, RootTab rt) {
+  EncArgs<F> a;
+  a.leaves = d.leaves;
+  a.msg_len = d.msg_len;
+  a.M = (int)d.n_msgs;
+  a.logC = d.plan.logC;
+  a.logN = d.plan.logN;
+  a.logC1 = d.plan.logC1;
+  a.logC2 = d.plan.logC2;
+  a.K = 1ull << (d.plan.logN - d.plan.logC);
+  a.G = d.plan.cosets_per_cta;
+  a.W = d.plan.cols_per_cta;
+  a.rt = rt;
+  return a;
+}
+
+template <class F>
+int encode_multi_prepare(const EncodeJobDesc* jobs, size_t njobs, RootTab rt, void* host_image,
+                         EncodeMultiLaunch* out) {
+  EncodeMultiLaunch l{};
+  l.rows_off = (njobs * sizeof(EncJob<F>) + 15) & ~(size_t)15;
+  l.bytes = l.rows_off + njobs * sizeof(EncJob<F>);
+  EncJob<F>* cols = reinterpret_cast<EncJob<F>*>(host_image);
+  EncJob<F>* rows = reinterpret_cast<EncJob<F>*>(static_cast<uint8_t*>(host_image) + l.rows_off);
+  for (size_t i = 0; i < njobs; ++i) {
+    const EncodeJobDesc& d = jobs[i];
+    const EncodePlan& p = d.plan;
+    if (p.logN > rt.log_order || p.logN > 32) return WHIR_ERR_UNSUPPORTED;
+    EncArgs<F> a = enc_args_of<F>(d, rt);
+    const F* src = static_cast<const F*>(d.src);
+    F* scratch = static_cast<F*>(d.scratch);
+    if (p.mode == 0) {
+      a.mode = 0;
+      a.src = src;
+      a.dst = static_cast<F*>(d.dst);
+      const size_t n = 1ull << p.logC;
+      l.rows_smem = std::max(l.rows_smem, (size_t)a.G * d.n_msgs * n * sizeof(F) + n * sizeof(typename F::Base) + 16);
+      rows[l.nrows].args = a;
+      rows[l.nrows].cta_begin = l.rows_grid;
+      l.rows_grid += a.K / a.G;
+      ++l.nrows;
+    } else {
+      const size_t C1 = 1ull << p.logC1, C2 = 1ull << p.logC2;
+      EncArgs<F> c = a;
+      c.src = src;
+      c.dst = scratch;
+      c.leaves = nullptr;
+      c.mode = 1;
+      l.cols_smem = std::max(l.cols_smem, (size_t)a.W * C1 * sizeof(F) + 16);
+      cols[l.ncols].args = c;
+      cols[l.ncols].cta_begin = l.cols_grid;
+      l.cols_grid += d.n_msgs * a.K * (C2 / a.W);
+      ++l.ncols;
+      a.mode = 1;
+      a.src = scratch;
+      a.dst = static_cast<F*>(d.dst);
+      l.rows_smem = std::max(l.rows_smem, d.n_msgs * C2 * sizeof(F) + C2 * sizeof(typename F::Base) + 16);
+      rows[l.nrows].args = a;
+      rows[l.nrows].cta_begin = l.rows_grid;
+      l.rows_grid += a.K * C1;
+      ++l.nrows;
+    }
+  }
+  if (l.cols_grid > 0x7fffffffull || l.rows_grid > 0x7fffffffull) return WHIR_ERR_UNSUPPORTED;
+  if (l.cols_smem > ENC_SMEM_ATTR || l.rows_smem > ENC_SMEM_ATTR) return WHIR_ERR_UNSUPPORTED;
+  *out = l;
+  return 0;
+}
+
+template <class F, int KIND>
+static cudaError_t run_rows_multi(const EncJob<F>* tab, int n, unsigned grid, size_t smem, cudaStream_t s) {
+  static std::once_flag flags[ENC_MAX_DEVICES];
+  static cudaError_t results[ENC_MAX_DEVICES];
+  cudaError_t e = smem_attr_once(encode_rows_multi_kernel<F, KIND>, flags, results);
+  if (e != cudaSuccess) return e;
+  encode_rows_multi_kernel<F, KIND><<<grid, ENC_THREADS, smem, s>>>(tab, n);
+  note_launch();
+  return cudaGetLastError();
+}
+
+template <class F>
+cudaError_t launch_encode_multi(const EncodeMultiLaunch& l, const void* dev_image, int hash_kind, cudaStream_t s) {
+  const EncJob<F>* cols = static_cast<const EncJob<F>*>(dev_image);
+  const EncJob<F>* rows =
+      reinterpret_cast<const EncJob<F>*>(static_cast<const uint8_t*>(dev_image) + l.rows_off);
+  if (l.ncols) {
+    static std::once_flag flags[ENC_MAX_DEVICES];
+    static cudaError_t results[ENC_MAX_DEVICES];
+    cudaError_t e = smem_attr_once(encode_cols_multi_kernel<F>, flags, results);
+    if (e != cudaSuccess) return e;
+    encode_cols_multi_kernel<F><<<(unsigned)l.cols_grid, ENC_THREADS, l.cols_smem, s>>>(cols, l.ncols);
+    note_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  if (!l.nrows) return cudaSuccess;
+  const unsigned g = (unsigned)l.rows_grid;
+  switch (hash_kind) {
+    case HASH_BLAKE3: return run_rows_multi<F, HASH_BLAKE3>(rows, l.nrows, g, l.rows_smem, s);
+    case HASH_SHA2: return run_rows_multi<F, HASH_SHA2>(rows, l.nrows, g, l.rows_smem, s);
+    case HASH_SHA3: return run_rows_multi<F, HASH_SHA3>(rows, l.nrows, g, l.rows_smem, s);
+    case HASH_KECCAK: return run_rows_multi<F, HASH_KECCAK>(rows, l.nrows, g, l.rows_smem, s);
+    default: return run_rows_multi<F, HASH_COPY>(rows, l.nrows, g, l.rows_smem, s);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
 // Opening gathers
 // ---------------------------------------------------------------------------------------------
 template <class F>
@@ -563,6 +725,9 @@ cudaError_t launch_to_canonical(F* v, size_t n, cudaStream_t s) {
 #define WHIR_ENCODE_INST(F)                                                                                      \
   template cudaError_t launch_encode<F>(const EncodePlan&, const F*, size_t, size_t, F*, uint32_t*, int, F*, RootTab, \
                                         cudaStream_t, const EncodeStaging*);                                     \
+  template size_t encode_multi_table_bytes<F>(size_t);                                                           \
+  template int encode_multi_prepare<F>(const EncodeJobDesc*, size_t, RootTab, void*, EncodeMultiLaunch*);        \
+  template cudaError_t launch_encode_multi<F>(const EncodeMultiLaunch&, const void*, int, cudaStream_t);         \
   template cudaError_t launch_gather_rows<F>(const F*, size_t, const uint64_t*, size_t, F*, cudaStream_t);       \
   template cudaError_t launch_to_internal<F>(F*, size_t, cudaStream_t);                                         \
   template cudaError_t launch_to_canonical<F>(F*, size_t, cudaStream_t);

@@ -7,6 +7,8 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <string>
+#include <vector>
 
 #include "field.cuh"
 
@@ -45,9 +47,29 @@ struct EncodePlan {
   size_t scratch_elems;  // intermediate elements needed by mode 1
 };
 
-// Plans an encode of n_msgs messages of msg_len elements (elem_bytes each) into codeword_len rows.
-// Returns 0, or a negative status when the shape is unsupported on the device.
+// Plans an encode of n_msgs messages of msg_len elements (elem_bytes each) into codeword_len rows:
+// the autotuned choice for the shape when one is recorded (encode_tuning_set), else the default
+// heuristics (plan_encode_default). Returns 0, or a negative status when the shape is unsupported.
 int plan_encode(size_t n_msgs, size_t msg_len, size_t codeword_len, size_t elem_bytes, EncodePlan* plan);
+int plan_encode_default(size_t n_msgs, size_t msg_len, size_t codeword_len, size_t elem_bytes, EncodePlan* plan);
+// Explicit plan choices: mode 0 with G cosets per CTA, or mode 1 with a 2^logC2-point row pass and
+// W columns per column-pass CTA.
+struct EncodeTuning {
+  int mode, logC2, W, G;
+};
+int plan_encode_tuned(size_t n_msgs, size_t msg_len, size_t codeword_len, size_t elem_bytes, const EncodeTuning& t,
+                      EncodePlan* plan);
+// Process-wide table of tuned choices (encode plans by shape, Merkle tile heights by tree height),
+// written by the autotuner, exported and imported as text lines
+//   "encode <n_msgs> <msg_len> <codeword_len> <elem_bytes> <mode> <logC2> <W> <G>"
+//   "merkle <layers> <tile_log>"
+void encode_tuning_set(size_t n_msgs, size_t msg_len, size_t codeword_len, size_t elem_bytes, const EncodeTuning& t);
+bool encode_tuning_get(size_t n_msgs, size_t msg_len, size_t codeword_len, size_t elem_bytes, EncodeTuning* t);
+void merkle_tuning_set(int layers, int tile_log);
+int merkle_tile_log_for(int layers);
+std::string tuning_export();
+int tuning_import(const char* text);
+void tuning_clear();
 
 // Messages made resident by work on another stream, in `groups` consecutive message groups:
 // group g holds messages [bounds[g], bounds[g + 1]) (bounds[0] = 0, bounds[groups] = n_msgs), and
@@ -68,9 +90,53 @@ cudaError_t launch_encode(const EncodePlan& plan, const F* src, size_t n_msgs, s
                           uint32_t* leaves, int hash_kind, F* scratch, RootTab rt, cudaStream_t s,
                           const EncodeStaging* staging = nullptr);
 
+// Several independent interleaved encodes (jobs of possibly different shapes, one field) in one
+// launch per pass: the CTAs of a launch are split among the jobs by a device table of per-job
+// arguments (encode_multi_prepare fills its host image; upload it, then launch_encode_multi).
+struct EncodeJobDesc {
+  EncodePlan plan;
+  const void* src;   // messages (device, message-major)
+  size_t n_msgs, msg_len;
+  void* dst;         // codeword (device, row-major)
+  uint32_t* leaves;  // leaf digests (device), or nullptr
+  void* scratch;     // four-step intermediate of plan.scratch_elems elements (mode 1 jobs)
+};
+struct EncodeMultiLaunch {
+  int ncols, nrows;             // jobs in the column pass (four-step jobs) and in the row pass
+  uint64_t cols_grid, rows_grid;
+  size_t cols_smem, rows_smem;  // dynamic shared memory (the largest job's)
+  size_t rows_off, bytes;       // byte offset of the row-pass table in the image; image size
+};
+template <class F>
+size_t encode_multi_table_bytes(size_t njobs);
+template <class F>
+int encode_multi_prepare(const EncodeJobDesc* jobs, size_t njobs, RootTab rt, void* host_image,
+                         EncodeMultiLaunch* out);
+template <class F>
+cudaError_t launch_encode_multi(const EncodeMultiLaunch& l, const void* dev_image, int hash_kind, cudaStream_t s);
+
+// Merkle trees of several jobs built together: each launch covers the tiles of every tree at the
+// same step (merkle_multi_plan lays out the table image to upload; launch_merkle_multi runs it).
+struct MerkleJobDesc {
+  uint32_t* nodes;
+  int layers;
+};
+struct MerkleMultiLaunch {
+  size_t offset;  // byte offset of the launch's table slice in the image
+  int n, S;       // trees in the launch, phase-A depth
+  uint64_t grid;
+};
+void merkle_multi_plan(const MerkleJobDesc* jobs, size_t njobs, int tile_log, std::vector<MerkleMultiLaunch>& launches,
+                       std::vector<uint8_t>& image);
+cudaError_t launch_merkle_multi(const std::vector<MerkleMultiLaunch>& launches, const void* dev_image, int hash_kind,
+                                cudaStream_t s);
+
 // Builds Merkle layers above the leaf layer in place. nodes: (2^(layers+1) - 1) digests laid out
-// [leaves (2^layers)][layer 1]...[root] (merkle_tree.rs:96-121).
-cudaError_t launch_merkle(uint32_t* nodes, int layers, int hash_kind, cudaStream_t s);
+// [leaves (2^layers)][layer 1]...[root] (merkle_tree.rs:96-121). Each launch hashes tiles of
+// 2^tile_log nodes up tile_log layers (tile_log <= 0: the tuned height for this tree, or
+// merkle_tile_log, 10, when none is recorded).
+cudaError_t launch_merkle(uint32_t* nodes, int layers, int hash_kind, cudaStream_t s, int tile_log = 0);
+extern int merkle_tile_log;
 
 // count messages of `size` bytes (size % 4 == 0) -> count digests.
 cudaError_t launch_hash_many(const uint8_t* in, size_t size, size_t count, uint8_t* out, int hash_kind,
@@ -211,16 +277,20 @@ static constexpr int TS_MAX_FORMS = 4;
 static constexpr int TS_MAX_RPC = 32;  // rows per CTA in the sums pass
 
 struct TensorShape {
-  int k, R, C;         // folded variables, row bits, column bits (n = k + R + C)
-  int nvec, nforms;    // vectors (RLC'd) and tensor forms
+  int k, R, C;          // folded variables, row bits, column bits (n = k + R + C)
+  int nvec, nforms;     // vectors (RLC'd) and tensor forms
   uint64_t vec_stride;  // elements between consecutive vectors
-  int rpc;             // rows per CTA (sums pass)
-  int threads;         // CTA threads (sums pass; a multiple of 32)
+  int rpc;              // rows per CTA (sums pass)
+  int cpt;              // adjacent columns per thread (sums pass; 2 for 8-byte source elements)
+  int threads;          // CTA threads (sums pass; a multiple of 32)
   uint64_t col_tiles, row_groups;
   uint64_t grid() const { return ((uint64_t)nvec << k) * row_groups * col_tiles; }
 };
 
-inline TensorShape tensor_plan(int nvars, int k, int nvec, int nforms, uint64_t vec_stride) {
+// src_bytes / src_aligned16: source element size and whether the vectors start on a 16-byte boundary
+// (two 8-byte columns per thread are read with one 16-byte load).
+inline TensorShape tensor_plan(int nvars, int k, int nvec, int nforms, uint64_t vec_stride, size_t src_bytes,
+                               bool src_aligned16) {
   TensorShape sh;
   sh.k = k;
   const int rest = nvars - k;
@@ -231,8 +301,9 @@ inline TensorShape tensor_plan(int nvars, int k, int nvec, int nforms, uint64_t 
   sh.vec_stride = vec_stride;
   sh.rpc = (int)std::min<uint64_t>(1ull << sh.R, TS_MAX_RPC);
   const uint64_t cols = 1ull << sh.C;
-  sh.threads = (int)std::max<uint64_t>(32, std::min<uint64_t>(TS_THREADS, cols));
-  sh.col_tiles = (cols + sh.threads - 1) / sh.threads;
+  sh.cpt = (src_bytes == 8 && src_aligned16 && cols >= 64 && vec_stride % 2 == 0) ? 2 : 1;
+  sh.threads = (int)std::max<uint64_t>(32, std::min<uint64_t>(TS_THREADS, cols / sh.cpt));
+  sh.col_tiles = (cols / sh.cpt + sh.threads - 1) / sh.threads;
   sh.row_groups = (1ull << sh.R) / sh.rpc;
   return sh;
 }

@@ -252,6 +252,12 @@ __global__ void __launch_bounds__(512) mail_copy_kernel(const uint8_t* s0, size_
   if (threadIdx.x == 0) *reinterpret_cast<volatile unsigned int*>(flag) = seq;
 }
 
+// out[j] = the root digest of tree j (its last node).
+__global__ void gather_roots_kernel(const uint32_t* const* roots, int n, uint32_t* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n * 8; i += gridDim.x * blockDim.x)
+    out[i] = roots[i >> 3][i & 7];
+}
+
 namespace {
 
 // Device -> host copy of up to two segments, in two halves so that the host can enqueue more work
@@ -627,6 +633,98 @@ std::unique_ptr<whir_witness> irs_commit(whir_ctx* ctx, const Irs& c, Transcript
   return w;
 }
 
+// Several commitments (Config::commit of independent jobs, irs_commit.rs:292-350) with the device
+// work of every job in shared launches: one column pass and one row pass (with the leaf hashes)
+// covering every job's encode through a per-job table, Merkle trees built step by step with every
+// job's tiles in one launch, and one fetch of all roots. The transcript steps (root, out-of-domain
+// samples) then follow per job, exactly as in irs_commit. Every job has the embedding S -> T and
+// commits with its own configuration cs[j].
+template <class S, class T>
+std::vector<std::unique_ptr<whir_witness>> irs_commit_batch(whir_ctx* ctx, const std::vector<const Irs*>& cs,
+                                                            const std::vector<Transcript*>& tss,
+                                                            const std::vector<const S*>& d_vecs, int field) {
+  const size_t n = cs.size();
+  std::vector<std::unique_ptr<whir_witness>> ws(n);
+  std::vector<EncodeJobDesc> enc(n);
+  std::vector<MerkleJobDesc> mk(n);
+  std::vector<DBuf<S>> scratch(n);
+  int kind = -1;
+  for (size_t j = 0; j < n; ++j) {
+    const Irs& c = *cs[j];
+    const int k = hash_kind_or_throw(c.hash_id);
+    if (kind >= 0 && k != kind) throw Error(WHIR_ERR_INVALID, "a batched commit needs one hash engine");
+    kind = k;
+    const size_t n_msgs = c.num_cols, msg_len = c.message_length(), cw = c.codeword_length;
+    if (n_msgs * msg_len != c.num_vectors * c.vector_size) throw Error(WHIR_ERR_UNSUPPORTED, "message matrix shape");
+    EncodePlan plan;
+    int rc = plan_encode(n_msgs, msg_len, cw, sizeof(S), &plan);
+    if (rc) throw Error(rc, "encode shape unsupported on the device");
+    if (kind == HASH_BLAKE3 && n_msgs * sizeof(S) > 1024)
+      throw Error(WHIR_ERR_UNSUPPORTED, "Blake3 leaves longer than one chunk (1024 bytes) are not supported");
+    if (kind == HASH_COPY && n_msgs * sizeof(S) > 32) throw Error(WHIR_ERR_INVALID, "Copy engine needs leaves <= 32 bytes");
+    auto w = std::make_unique<whir_witness>();
+    w->ctx = ctx;
+    w->field = field;
+    w->codeword_len = cw;
+    w->num_cols = n_msgs;
+    w->layers = layers_for(cw);
+    w->elem_limbs = S::LIMBS;
+    w->matrix = DBuf<uint64_t>(ctx, cw * n_msgs * S::LIMBS);
+    w->nodes = DBuf<uint32_t>(ctx, ((2ull << w->layers) - 1) * 8);
+    scratch[j] = DBuf<S>(ctx, plan.scratch_elems);
+    enc[j] = EncodeJobDesc{plan, d_vecs[j], n_msgs, msg_len, w->matrix.p, w->nodes.p, scratch[j].p};
+    mk[j] = MerkleJobDesc{w->nodes.p, (int)w->layers};
+    ws[j] = std::move(w);
+  }
+  if (n == 0) return ws;
+  {
+    ProfScope prof(ctx, PF_ENCODE);
+    std::vector<uint8_t> image(encode_multi_table_bytes<S>(n));
+    EncodeMultiLaunch l;
+    const int rc = encode_multi_prepare<S>(enc.data(), n, root_tab<typename S::Base>(ctx), image.data(), &l);
+    if (rc) throw Error(rc, "batched encode shape unsupported on the device");
+    DBuf<uint8_t> dimg(ctx, l.bytes);
+    h2d(ctx, dimg.p, image.data(), l.bytes);
+    CU(launch_encode_multi<S>(l, dimg.p, kind, ctx->stream));
+  }
+  DBuf<uint32_t> roots(ctx, n * 8);
+  {
+    ProfScope prof(ctx, PF_MERKLE);
+    std::vector<MerkleMultiLaunch> launches;
+    std::vector<uint8_t> image;
+    merkle_multi_plan(mk.data(), n, 0, launches, image);
+    DBuf<uint8_t> dimg(ctx, std::max<size_t>(image.size(), 1));
+    h2d(ctx, dimg.p, image.data(), image.size());
+    CU(launch_merkle_multi(launches, dimg.p, kind, ctx->stream));
+    std::vector<const uint32_t*> rp(n);
+    for (size_t j = 0; j < n; ++j) rp[j] = ws[j]->nodes.p + ((2ull << ws[j]->layers) - 2) * 8;
+    DBuf<const uint32_t*> drp(ctx, n);
+    h2d(ctx, drp.p, rp.data(), n * sizeof(const uint32_t*));
+    gather_roots_kernel<<<(unsigned)((n * 8 + 255) / 256), 256, 0, ctx->stream>>>(drp.p, (int)n, roots.p);
+    CU(cudaGetLastError());
+    note_launch();
+  }
+  std::vector<uint8_t> hroots(n * 32);
+  d2h(ctx, hroots.data(), roots.p, n * 32);
+  for (size_t j = 0; j < n; ++j) {
+    const Irs& c = *cs[j];
+    whir_witness& w = *ws[j];
+    memcpy(w.root, hroots.data() + j * 32, 32);
+    Transcript& ts = *tss[j];
+    ts.prover_bytes(w.root, 32);
+    for (size_t i = 0; i < c.out_domain_samples; ++i) put_raw(w.ood_points, challenge<T>(ts));
+    for (size_t i = 0; i < c.out_domain_samples; ++i) {
+      T pt = get_raw<T>(&w.ood_points[i * T::LIMBS]);
+      for (size_t v = 0; v < c.num_vectors; ++v) {
+        T val = univariate_device<T, S>(ctx, d_vecs[j] + v * c.vector_size, c.vector_size, pt);
+        send_elem<T>(ts, val);
+        put_raw(w.ood_matrix, val);
+      }
+    }
+  }
+  return ws;
+}
+
 // irs_commit::Config::open (irs_commit.rs:385-432) in two halves. irs_open_begin samples the query
 // indices, computes the evaluation points (and their root exponents), launches the row and sibling
 // gathers of every witness and starts their copy to the host; irs_open_end waits for the copy,
@@ -949,7 +1047,8 @@ std::vector<T> initial_sumcheck_tensor(whir_ctx* ctx, const Sumcheck& c, Transcr
   const int nvars = (int)layers_for(n);
   const int k = (int)c.num_rounds;
   const int NF = (int)forms.size();
-  const TensorShape sh = tensor_plan(nvars, k, (int)nvec, NF, n);
+  const TensorShape sh =
+      tensor_plan(nvars, k, (int)nvec, NF, n, sizeof(S), reinterpret_cast<uintptr_t>(x) % 16 == 0);
   const size_t rows = (size_t)1 << sh.R, cols = (size_t)1 << sh.C, per = rows + cols;
   const size_t nz = (size_t)1 << k;
   std::vector<T> rs;
@@ -1796,6 +1895,210 @@ int whir_commit(whir_ctx* ctx, const whir_config* cfg, whir_prover_state* ps, co
       return 0;
     });
   });
+}
+
+int whir_commit_batch(whir_ctx* ctx, size_t n, const whir_config* const* cfgs, whir_prover_state* const* pss,
+                      const uint64_t* const* vectors, uint32_t flags, whir_witness** out) {
+  return guarded([&] {
+    check_ctx(ctx);
+    if (n && (!cfgs || !pss || !vectors || !out)) throw Error(WHIR_ERR_INVALID, "null argument");
+    for (size_t j = 0; j < n; ++j) {
+      if (!cfgs[j] || !pss[j] || !vectors[j]) throw Error(WHIR_ERR_INVALID, "null job argument");
+      if (cfgs[j]->cfg.field != cfgs[0]->cfg.field) throw Error(WHIR_ERR_INVALID, "a batched commit needs one field");
+      if (pss[j]->cfg != cfgs[j]) throw Error(WHIR_ERR_INVALID, "prover state of another configuration");
+      out[j] = nullptr;
+    }
+    if (n == 0) return 0;
+    return with_embedding(cfgs[0]->cfg.field, [&]<class S, class T>() {
+      std::vector<const Irs*> cs(n);
+      std::vector<Transcript*> tss(n);
+      std::vector<const S*> dv(n);
+      std::vector<DBuf<S>> copies(n);
+      for (size_t j = 0; j < n; ++j) {
+        const Config& c = cfgs[j]->cfg;
+        cs[j] = &c.initial;
+        tss[j] = &pss[j]->ts;
+        dv[j] = device_vectors<S>(ctx, vectors[j], c.initial.num_vectors * c.size(), flags, copies[j], false);
+      }
+      auto ws = irs_commit_batch<S, T>(ctx, cs, tss, dv, cfgs[0]->cfg.field);
+      CU(cudaStreamSynchronize(ctx->stream));
+      for (size_t j = 0; j < n; ++j) {
+        if (!(flags & WHIR_DEVICE_PTRS)) {
+          // Keep the device copy: prove() given the same host buffer reuses it.
+          ws[j]->host_src = vectors[j];
+          ws[j]->vectors = DBuf<uint64_t>();
+          ws[j]->vectors.ctx = ctx;
+          ws[j]->vectors.p = reinterpret_cast<uint64_t*>(copies[j].p);
+          ws[j]->vectors.n = copies[j].n * S::LIMBS;
+          copies[j].p = nullptr;
+        }
+      }
+      for (size_t j = 0; j < n; ++j) out[j] = ws[j].release();
+      return 0;
+    });
+  });
+}
+
+// ---- autotuner ---------------------------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+
+// Event-timed minimum over `reps` runs of fn() on the context's stream (milliseconds).
+template <class Fn>
+double time_min(whir_ctx* ctx, int reps, Fn&& fn) {
+  cudaEvent_t e0 = take_event(ctx), e1 = take_event(ctx);
+  double best = 1e30;
+  for (int r = 0; r < reps; ++r) {
+    CU(cudaEventRecord(e0, ctx->stream));
+    fn();
+    CU(cudaEventRecord(e1, ctx->stream));
+    CU(cudaEventSynchronize(e1));
+    float ms = 0;
+    CU(cudaEventElapsedTime(&ms, e0, e1));
+    best = std::min(best, (double)ms);
+  }
+  ctx->event_pool.push_back(e0);
+  ctx->event_pool.push_back(e1);
+  return best;
+}
+
+// Tunes the encode plan of one commitment shape (elements of F) and the Merkle tile height of its
+// tree: every valid candidate is timed on the device and the fastest is recorded in the process-wide
+// table that plan_encode / launch_merkle consult. Appends a JSON object to `report`.
+template <class F>
+void autotune_shape(whir_ctx* ctx, size_t n_msgs, size_t msg_len, size_t cw, int kind, int reps, std::string& report) {
+  std::vector<std::pair<EncodeTuning, EncodePlan>> cands;
+  size_t C = 1;
+  while (C < msg_len) C <<= 1;
+  const int logC = (int)layers_for(C);
+  for (int G = 1; G <= 64; G *= 2) {
+    EncodePlan p;
+    EncodeTuning t{0, 0, 0, G};
+    if (plan_encode_tuned(n_msgs, msg_len, cw, sizeof(F), t, &p) == 0) cands.push_back({t, p});
+  }
+  for (int l2 = 1; l2 < logC; ++l2)
+    for (int W = 1; W <= 64; W *= 2) {
+      EncodePlan p;
+      EncodeTuning t{1, l2, W, 1};
+      if (plan_encode_tuned(n_msgs, msg_len, cw, sizeof(F), t, &p) == 0) cands.push_back({t, p});
+    }
+  EncodePlan def;
+  if (plan_encode_default(n_msgs, msg_len, cw, sizeof(F), &def)) return;
+  size_t scratch_elems = 0;
+  for (auto& c : cands) scratch_elems = std::max(scratch_elems, c.second.scratch_elems);
+  const size_t layers = layers_for(cw);
+  DBuf<F> src(ctx, std::max<size_t>(n_msgs * msg_len, 1)), dst(ctx, cw * n_msgs), scratch(ctx, scratch_elems);
+  DBuf<uint32_t> nodes(ctx, ((2ull << layers) - 1) * 8);
+  CU(cudaMemsetAsync(src.p, 0, std::max<size_t>(n_msgs * msg_len, 1) * sizeof(F), ctx->stream));
+  CU(cudaMemsetAsync(nodes.p, 0, ((2ull << layers) - 1) * 32, ctx->stream));
+  const RootTab rt = root_tab<typename F::Base>(ctx);
+  double best = 1e30, def_ms = 0;
+  EncodeTuning pick{};
+  char buf[200];
+  report += "{\"n_msgs\":" + std::to_string(n_msgs) + ",\"msg_len\":" + std::to_string(msg_len) +
+            ",\"codeword_len\":" + std::to_string(cw) + ",\"elem_bytes\":" + std::to_string(sizeof(F)) +
+            ",\"candidates\":[";
+  bool first = true;
+  for (auto& c : cands) {
+    const double ms = time_min(ctx, reps, [&] {
+      CU(launch_encode<F>(c.second, src.p, n_msgs, msg_len, dst.p, nodes.p, kind, scratch.p, rt, ctx->stream));
+    });
+    snprintf(buf, sizeof(buf), "%s[%d,%d,%d,%d,%.4f]", first ? "" : ",", c.first.mode, c.first.logC2, c.first.W,
+             c.first.G, ms);
+    report += buf;
+    first = false;
+    const bool is_def = c.second.mode == def.mode && c.second.logC2 == def.logC2 &&
+                        c.second.cols_per_cta == def.cols_per_cta && c.second.cosets_per_cta == def.cosets_per_cta;
+    if (is_def) def_ms = ms;
+    if (ms < best) {
+      best = ms;
+      pick = c.first;
+    }
+  }
+  if (!cands.empty()) encode_tuning_set(n_msgs, msg_len, cw, sizeof(F), pick);
+  snprintf(buf, sizeof(buf), "],\"pick\":[%d,%d,%d,%d],\"pick_ms\":%.4f,\"default_ms\":%.4f", pick.mode,
+           pick.logC2, pick.W, pick.G, best, def_ms);
+  report += buf;
+  // Merkle tile height for this tree
+  int best_tl = merkle_tile_log;
+  double mbest = 1e30;
+  report += ",\"merkle\":[";
+  first = true;
+  for (int tl = 6; tl <= 10; ++tl) {
+    const double ms = time_min(ctx, reps, [&] { CU(launch_merkle(nodes.p, (int)layers, kind, ctx->stream, tl)); });
+    snprintf(buf, sizeof(buf), "%s[%d,%.4f]", first ? "" : ",", tl, ms);
+    report += buf;
+    first = false;
+    if (ms < mbest) {
+      mbest = ms;
+      best_tl = tl;
+    }
+  }
+  merkle_tuning_set((int)layers, best_tl);
+  snprintf(buf, sizeof(buf), "],\"merkle_pick\":%d}", best_tl);
+  report += buf;
+}
+
+}  // namespace
+
+extern "C" {
+
+int whir_autotune(whir_ctx* ctx, const whir_config* cfg, int reps, char* report, size_t cap) {
+  return guarded([&] {
+    check_ctx(ctx);
+    if (!cfg) throw Error(WHIR_ERR_INVALID, "null config");
+    const Config& c = cfg->cfg;
+    reps = std::max(1, std::min(reps, 20));
+    return with_embedding(c.field, [&]<class S, class T>() {
+      std::string rep = "{\"shapes\":[";
+      const int kind = hash_kind_or_throw(c.initial.hash_id);
+      autotune_shape<S>(ctx, c.initial.num_cols, c.initial.message_length(), c.initial.codeword_length, kind, reps, rep);
+      for (const Round& r : c.rounds) {
+        rep += ",";
+        autotune_shape<T>(ctx, r.irs.num_cols, r.irs.message_length(), r.irs.codeword_length,
+                          hash_kind_or_throw(r.irs.hash_id), reps, rep);
+      }
+      rep += "]}";
+      CU(cudaStreamSynchronize(ctx->stream));
+      if (report && cap) {
+        const size_t m = std::min(cap - 1, rep.size());
+        memcpy(report, rep.data(), m);
+        report[m] = 0;
+        if (rep.size() >= cap) throw Error(WHIR_ERR_INVALID, "report buffer too small");
+      }
+      return 0;
+    });
+  });
+}
+
+int whir_autotune_export(char* buf, size_t cap, size_t* len) {
+  return guarded([&] {
+    if (!len) throw Error(WHIR_ERR_INVALID, "null argument");
+    const std::string s = tuning_export();
+    *len = s.size();
+    if (buf && cap) {
+      const size_t m = std::min(cap - 1, s.size());
+      memcpy(buf, s.data(), m);
+      buf[m] = 0;
+      if (s.size() >= cap) throw Error(WHIR_ERR_INVALID, "buffer too small");
+    }
+    return 0;
+  });
+}
+
+int whir_autotune_import(const char* text) {
+  return guarded([&] {
+    if (!text) throw Error(WHIR_ERR_INVALID, "null argument");
+    const int rc = tuning_import(text);
+    if (rc) throw Error(rc, "malformed or invalid tuning line");
+    return 0;
+  });
+}
+
+int whir_autotune_clear(void) {
+  tuning_clear();
+  return 0;
 }
 
 int whir_witness_free(whir_witness* w) {

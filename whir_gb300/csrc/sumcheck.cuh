@@ -898,11 +898,27 @@ cudaError_t launch_rows_finish(T* a, size_t m, T r, const T* F, int rlog, const 
 // 2^R rows and 2^C columns; per form, `tables` holds the row weights (2^R) then the column weights
 // (2^C) of the tensor over variables k.. n-1.
 // ---------------------------------------------------------------------------------------------
-// Sums pass. CTA (j, z, row group g, column tile): thread = one column, rows [g rpc, (g+1) rpc) of
-// the z block; per form the thread accumulates sum_rows row_w[H] x(H, col) unreduced, then
-// multiplies by its column weight; the CTA's per-form sums go to partials, and the last CTA adds the
-// partials of every (j, f, z) into out[(j nforms + f) 2^k + z].
-template <class T, class S, int NF>
+// Loads CPT consecutive source elements (CPT == 2: one 16-byte load of two 8-byte elements).
+template <class S, int CPT>
+__device__ __forceinline__ void load_cols(const S* p, S* out) {
+  if constexpr (CPT == 2 && sizeof(S) == 8) {
+    const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(p);
+    reinterpret_cast<uint64_t*>(out)[0] = v.x;
+    reinterpret_cast<uint64_t*>(out)[1] = v.y;
+  } else {
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) out[c] = p[c];
+  }
+}
+
+// Sums pass. CTA (j, z, row group g, column tile): thread = CPT adjacent columns, rows
+// [g rpc, (g+1) rpc) of the z block; per form the thread accumulates sum_rows row_w[H] x(H, col)
+// unreduced, then multiplies by its column weight; the CTA's per-form sums go to partials, and the
+// last CTA adds the partials of every (j, f, z) into out[(j nforms + f) 2^k + z]. Rows are read in
+// batches of TS_RB, the next batch's loads issued before the current batch is multiplied (the first
+// version, one column per thread and no prefetch, ran at 16 % of DRAM peak, long-scoreboard bound).
+static constexpr int TS_RB = 4;
+template <class T, class S, int NF, int CPT>
 __global__ void __launch_bounds__(TS_THREADS) tensor_sums_kernel(const S* x, TensorShape sh, const T* tables,
                                                                  T* partials, T* out, unsigned int* counter) {
   __shared__ T srow[NF][TS_MAX_RPC];
@@ -914,37 +930,65 @@ __global__ void __launch_bounds__(TS_THREADS) tensor_sums_kernel(const S* x, Ten
   const uint64_t g = bid % sh.row_groups;
   bid /= sh.row_groups;
   const uint64_t z = bid & ((1ull << sh.k) - 1), j = bid >> sh.k;
-  const uint64_t col = tile * blockDim.x + threadIdx.x;
+  const uint64_t col = (tile * blockDim.x + threadIdx.x) * CPT;
   const uint64_t r0 = g * sh.rpc;
   for (int e = threadIdx.x; e < NF * sh.rpc; e += blockDim.x) {
     const int f = e / sh.rpc, r = e - f * sh.rpc;
     srow[f][r] = tables[(uint64_t)f * per + r0 + r];
   }
   __syncthreads();
-  WideAcc<T> acc[NF];
+  WideAcc<T> acc[NF][CPT];
 #pragma unroll
-  for (int f = 0; f < NF; ++f) acc[f].init();
+  for (int f = 0; f < NF; ++f)
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) acc[f][c].init();
   if (col < cols) {
     const S* base = x + j * sh.vec_stride + ((z << sh.R) + r0) * cols + col;
-    int r = 0;
-    for (; r + 8 <= sh.rpc; r += 8) {
-      S v[8];
+    const int full = sh.rpc / TS_RB * TS_RB;
+    S cur[TS_RB][CPT], nxt[TS_RB][CPT];
+    if (full) {
 #pragma unroll
-      for (int u = 0; u < 8; ++u) v[u] = base[(uint64_t)(r + u) * cols];
-#pragma unroll
-      for (int u = 0; u < 8; ++u)
-#pragma unroll
-        for (int f = 0; f < NF; ++f) acc[f].mac_mixed(srow[f][r + u], v[u]);
+      for (int u = 0; u < TS_RB; ++u) load_cols<S, CPT>(base + (uint64_t)u * cols, cur[u]);
     }
-    for (; r < sh.rpc; ++r) {
-      const S v = base[(uint64_t)r * cols];
+    for (int r = 0; r < full; r += TS_RB) {
+      const bool more = r + TS_RB < full;
+      if (more) {
 #pragma unroll
-      for (int f = 0; f < NF; ++f) acc[f].mac_mixed(srow[f][r], v);
+        for (int u = 0; u < TS_RB; ++u) load_cols<S, CPT>(base + (uint64_t)(r + TS_RB + u) * cols, nxt[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < TS_RB; ++u)
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          const T w = srow[f][r + u];
+#pragma unroll
+          for (int c = 0; c < CPT; ++c) acc[f][c].mac_mixed(w, cur[u][c]);
+        }
+      if (more) {
+#pragma unroll
+        for (int u = 0; u < TS_RB; ++u)
+#pragma unroll
+          for (int c = 0; c < CPT; ++c) cur[u][c] = nxt[u][c];
+      }
+    }
+    for (int r = full; r < sh.rpc; ++r) {
+      S v[CPT];
+      load_cols<S, CPT>(base + (uint64_t)r * cols, v);
+#pragma unroll
+      for (int f = 0; f < NF; ++f)
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) acc[f][c].mac_mixed(srow[f][r], v[c]);
     }
   }
   T mine[NF];
 #pragma unroll
-  for (int f = 0; f < NF; ++f) mine[f] = col < cols ? tables[(uint64_t)f * per + rows + col] * acc[f].get() : T::zero();
+  for (int f = 0; f < NF; ++f) {
+    mine[f] = T::zero();
+    if (col < cols) {
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) mine[f] += tables[(uint64_t)f * per + rows + col + c] * acc[f][c].get();
+    }
+  }
 #pragma unroll
   for (int f = 0; f < NF; ++f) {
     const T s = block_sum(mine[f]);
@@ -1024,13 +1068,21 @@ template <class T, class S>
 cudaError_t launch_tensor_sums(const S* x, const TensorShape& sh, const T* tables, T* partials, T* out,
                                unsigned int* counter, cudaStream_t s) {
   const unsigned grid = (unsigned)sh.grid();
+  const bool two = sh.cpt == 2;
+  if (two && (sizeof(S) != 8 || reinterpret_cast<uintptr_t>(x) % 16)) return cudaErrorInvalidValue;
+#define WHIR_TS_LAUNCH(NF)                                                                                        \
+  if (two)                                                                                                        \
+    tensor_sums_kernel<T, S, NF, 2><<<grid, sh.threads, 0, s>>>(x, sh, tables, partials, out, counter);          \
+  else                                                                                                            \
+    tensor_sums_kernel<T, S, NF, 1><<<grid, sh.threads, 0, s>>>(x, sh, tables, partials, out, counter);
   switch (sh.nforms) {
-    case 1: tensor_sums_kernel<T, S, 1><<<grid, sh.threads, 0, s>>>(x, sh, tables, partials, out, counter); break;
-    case 2: tensor_sums_kernel<T, S, 2><<<grid, sh.threads, 0, s>>>(x, sh, tables, partials, out, counter); break;
-    case 3: tensor_sums_kernel<T, S, 3><<<grid, sh.threads, 0, s>>>(x, sh, tables, partials, out, counter); break;
-    case 4: tensor_sums_kernel<T, S, 4><<<grid, sh.threads, 0, s>>>(x, sh, tables, partials, out, counter); break;
+    case 1: WHIR_TS_LAUNCH(1) break;
+    case 2: WHIR_TS_LAUNCH(2) break;
+    case 3: WHIR_TS_LAUNCH(3) break;
+    case 4: WHIR_TS_LAUNCH(4) break;
     default: return cudaErrorInvalidValue;
   }
+#undef WHIR_TS_LAUNCH
   note_launch();
   return cudaGetLastError();
 }

@@ -22,7 +22,7 @@ import time
 import numpy as np
 
 from . import (FIELDS, SOURCE_LIMBS, TARGET_LIMBS, Config, Context, ProtocolParameters, ProverState,
-               multilinear_evaluate)
+               commit_batch, multilinear_evaluate)
 from .inputs import Rng, field_elements
 
 BASE_OF = {"Goldilocks1": "Goldilocks1", "Goldilocks2": "Goldilocks1", "Goldilocks3": "Goldilocks1"}
@@ -88,12 +88,34 @@ def prove_job(ctx, job):
     return job
 
 
+def prove_jobs_batched(ctx, jobs):
+    """Commits `jobs` (one embedding and hash engine) in shared device launches (commit_batch: one
+    encode pass pair and one Merkle launch per tile step for all of them), then proves each from its
+    witness. Proof bytes equal prove_job's for every job."""
+    cfgs = [Config(j.field, j.size, j.params) for j in jobs]
+    states = [ProverState(c, j.session) for c, j in zip(cfgs, jobs)]
+    flats = [j.vectors.reshape(-1) for j in jobs]
+    wits = commit_batch(ctx, cfgs, states, flats)
+    for j, c, ps, flat, w in zip(jobs, cfgs, states, flats, wits):
+        c.prove(ctx, ps, flat, [w], j.points, [], j.evaluations)
+        w.free()
+        j.narg, j.hints = ps.proof()
+    return jobs
+
+
 class BatchProver:
-    def __init__(self, device=0, workers=8):
+    """Proves many jobs over `workers` contexts. With batch_commit, each worker takes a share of the
+    jobs (balanced by size), commits its share at once through commit_batch, then proves them in
+    turn; otherwise every job is committed and proved on its own."""
+
+    def __init__(self, device=0, workers=8, batch_commit=False):
         self.contexts = [Context(device) for _ in range(workers)]
+        self.batch_commit = batch_commit
 
     def prove_all(self, jobs):
         """Proves every job; returns them in the given order (results in job.narg / job.hints)."""
+        if self.batch_commit:
+            return self._prove_all_batched(jobs)
         order = sorted(range(len(jobs)), key=lambda i: -jobs[i].size)
         lock = threading.Lock()
         next_idx = [0]
@@ -109,6 +131,52 @@ class BatchProver:
                 try:
                     prove_job(ctx, jobs[i])
                 except Exception as e:  # surfaced after all workers stop
+                    with lock:
+                        errors.append(e)
+                    return
+
+        threads = [threading.Thread(target=worker, args=(c,)) for c in self.contexts]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        if errors:
+            raise errors[0]
+        return jobs
+
+    def _prove_all_batched(self, jobs):
+        # Groups of one embedding and hash engine, split into one chunk per worker of similar total
+        # size (largest job first into the lightest chunk): a worker commits its chunk in shared
+        # launches, then proves its jobs.
+        groups = collections.defaultdict(list)
+        for i, j in enumerate(jobs):
+            groups[(j.field, bytes(j.params.hash_id))].append(i)
+        chunks = []
+        for idx in groups.values():
+            idx.sort(key=lambda i: -jobs[i].size)
+            nchunks = max(1, min(len(self.contexts), len(idx)))
+            parts = [[] for _ in range(nchunks)]
+            loads = [0] * nchunks
+            for i in idx:
+                k = loads.index(min(loads))
+                parts[k].append(i)
+                loads[k] += jobs[i].size
+            chunks += [p for p in parts if p]
+        chunks.sort(key=lambda p: -sum(jobs[i].size for i in p))
+        lock = threading.Lock()
+        nxt = [0]
+        errors = []
+
+        def worker(ctx):
+            while True:
+                with lock:
+                    if nxt[0] >= len(chunks) or errors:
+                        return
+                    part = chunks[nxt[0]]
+                    nxt[0] += 1
+                try:
+                    prove_jobs_batched(ctx, [jobs[i] for i in part])
+                except Exception as e:
                     with lock:
                         errors.append(e)
                     return
