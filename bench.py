@@ -53,6 +53,7 @@ def parse_args():
                     help="d of the CPU-baseline proofs (default: --nv, the measured workload itself)")
     ap.add_argument("--cpu-runs", type=int, default=5, help="timed CPU-baseline proofs (after one warm-up)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default encode plans and Merkle tiles")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched / serving measurements")
     ap.add_argument("--batch-jobs", type=int, default=64)
@@ -180,12 +181,22 @@ def batched_and_serving(args, dev):
     batch_s, batch_passes = median_pass_s(many, jobs)
     many.close()
     same = all((j.narg, j.hints) == r for j, r in zip(jobs, ref))
+    # Batched commits: each worker commits its share of the jobs in shared launches (one encode pass
+    # pair and one Merkle launch per tile step over a job table), then proves them.
+    bc = serving.BatchProver(dev, workers=args.workers, batch_commit=True)
+    bc.prove_all(jobs[:8])
+    bc_s, bc_passes = median_pass_s(bc, jobs)
+    bc.close()
+    same_bc = all((j.narg, j.hints) == r for j, r in zip(jobs, ref))
     out["batched"] = {
         "workload": "%d x WHIR commit+prove, Goldilocks3, d in {14,16,18,20,22}, Blake3, rate 1/2, k=4, sec 128 "
                     "list decoding, 1-2 points" % len(jobs),
         "proofs_per_s": len(jobs) / batch_s, "back_to_back_proofs_per_s": len(jobs) / plain_s,
-        "speedup_vs_back_to_back": plain_s / batch_s, "workers": args.workers, "bit_exact_vs_plain": same,
+        "speedup_vs_back_to_back": plain_s / batch_s, "workers": args.workers,
+        "bit_exact_vs_plain": same and same_bc,
         "passes_proofs_per_s": [len(jobs) / t for t in batch_passes],
+        "batched_commit_proofs_per_s": len(jobs) / bc_s,
+        "batched_commit_passes_proofs_per_s": [len(jobs) / t for t in bc_passes],
         "timing": "host wall clock, median of 3 passes"}
     sjobs = serving.serving_workload(ctx, count=args.serve_jobs)
     cap = serving.BatchProver(dev, workers=args.workers)
@@ -415,6 +426,14 @@ def run_gpu(args):
         w.free()
         return ps
 
+    tuned = None
+    if not args.no_autotune:
+        # Encode plans and Merkle tile heights measured for this configuration's commitment shapes
+        # (whir_autotune); proofs are bit-identical under any choice.
+        rep = W.autotune(ctx, cfg, reps=3)
+        tuned = [{"shape": [s["n_msgs"], s["msg_len"], s["codeword_len"], s["elem_bytes"]], "pick": s["pick"],
+                  "pick_ms": s["pick_ms"], "default_ms": s["default_ms"], "merkle_tile_log": s["merkle_pick"]}
+                 for s in rep["shapes"]]
     ref_narg = None
     for _ in range(args.warmup):
         ps = one_proof(True, d_vec)
@@ -520,6 +539,7 @@ def run_gpu(args):
                    "p50_ms": float(np.percentile(times, 50)), "p99_ms": float(np.percentile(times, 99))},
         "roofline": roofline,
         "kernel_families_ms_per_proof": {k: v[0] / prof_steps for k, v in prof.items() if v[1]},
+        "autotune": tuned,
         "cpu_baseline": cpu,
         "bit_exact_vs_cpu": bit_exact,
         "e2e": e2e,

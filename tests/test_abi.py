@@ -119,3 +119,22 @@ def test_invalid_arguments_return_error_codes():
     pt = np.zeros((10, 2), np.uint64)
     assert not c.verify("s", b"", b"", 1, [pt], [], [[np.zeros(2, np.uint64)]])  # empty proof: rejected
     assert lib.whir_verify(None, None, 0, None, 0, None, 0, 1, None, 0, None, 0, None) < 0
+
+
+def test_autotune_table_import_export_without_device():
+    # The tuning table is host state: import validates each line (a plan the kernels cannot run is
+    # refused), export writes it back in a canonical order, clear empties it.
+    W.autotune_clear()
+    try:
+        W.autotune_import("encode 16 1048576 2097152 8 1 9 4 1\nmerkle 21 9\n")
+        assert W.autotune_export() == "encode 16 1048576 2097152 8 1 9 4 1\nmerkle 21 9\n"
+        for bad in ("encode 16 1048576 2097152 8 1 9 64 1\n",  # column-pass tile over the shared-memory budget
+                    "encode 16 1048576 2097152 8 0 0 0 1\n",   # a whole 2^20-point coset in one CTA
+                    "merkle 21 11\n", "nonsense\n"):
+            with pytest.raises(W.WhirError):
+                W.autotune_import(bad)
+        assert W.autotune_export() == "encode 16 1048576 2097152 8 1 9 4 1\nmerkle 21 9\n"
+        W.autotune_clear()
+        assert W.autotune_export() == ""
+    finally:
+        W.autotune_clear()
