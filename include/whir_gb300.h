@@ -91,6 +91,11 @@ int whir_ctx_profile(whir_ctx* ctx, double* ms, uint64_t* calls, size_t n_famili
  * resident in HBM between calls). */
 int whir_device_alloc(whir_ctx* ctx, size_t bytes, void** out);
 int whir_device_free(whir_ctx* ctx, void* ptr);
+/* Page-locked host memory (cudaHostAlloc, usable from every context): inputs handed to whir_commit
+ * / whir_prove from such buffers are copied by DMA at full link speed while the encode runs; from
+ * ordinary (pageable) memory the copy is staged by the driver and runs several times slower. */
+int whir_host_alloc(size_t bytes, void** out);
+int whir_host_free(void* ptr);
 int whir_memcpy_h2d(whir_ctx* ctx, void* dst, const void* src, size_t bytes);
 int whir_memcpy_d2h(whir_ctx* ctx, void* dst, const void* src, size_t bytes);
 

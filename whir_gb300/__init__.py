@@ -210,6 +210,35 @@ class Context:
             pass
 
 
+class _PinnedBuffer:
+    """Owner of a page-locked host allocation (whir_host_alloc), freed when the last view dies."""
+
+    def __init__(self, nbytes):
+        lib = load_library()
+        ptr = ctypes.c_void_p()
+        _check(lib.whir_host_alloc(ctypes.c_size_t(max(nbytes, 1)), ctypes.byref(ptr)))
+        self.ptr = ptr.value
+        self.nbytes = max(nbytes, 1)
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                load_library().whir_host_free(ctypes.c_void_p(self.ptr))
+                self.ptr = None
+        except Exception:
+            pass
+
+
+def pinned_empty(count, dtype=np.uint64):
+    """A numpy array of `count` elements in page-locked host memory (whir_host_alloc): commit / prove
+    inputs in such memory are uploaded by DMA while the encode runs."""
+    dt = np.dtype(dtype)
+    buf = _PinnedBuffer(count * dt.itemsize)
+    raw = (ctypes.c_uint8 * buf.nbytes).from_address(buf.ptr)
+    raw._owner = buf  # keeps the allocation alive as long as any view of it
+    return np.frombuffer(raw, dtype=dt, count=count)
+
+
 class Witness:
     """irs_commit::Witness with the codeword and Merkle tree resident on the device."""
 

@@ -1734,6 +1734,26 @@ int whir_device_free(whir_ctx* ctx, void* ptr) {
     return 0;
   });
 }
+int whir_host_alloc(size_t bytes, void** out) {
+  return guarded([&] {
+    if (!out) throw Error(WHIR_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (bytes == 0) return 0;
+    cudaError_t e = cudaHostAlloc(out, bytes, cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+      *out = nullptr;
+      throw Error(e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ? WHIR_ERR_NO_DEVICE : WHIR_ERR_CUDA,
+                  std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
+    }
+    return 0;
+  });
+}
+int whir_host_free(void* ptr) {
+  return guarded([&] {
+    if (ptr) CU(cudaFreeHost(ptr));
+    return 0;
+  });
+}
 int whir_memcpy_h2d(whir_ctx* ctx, void* dst, const void* src, size_t bytes) {
   return guarded([&] {
     check_ctx(ctx);

@@ -22,7 +22,7 @@ import time
 import numpy as np
 
 from . import (FIELDS, SOURCE_LIMBS, TARGET_LIMBS, Config, Context, ProtocolParameters, ProverState,
-               commit_batch, multilinear_evaluate)
+               commit_batch, multilinear_evaluate, pinned_empty)
 from .inputs import Rng, field_elements
 
 BASE_OF = {"Goldilocks1": "Goldilocks1", "Goldilocks2": "Goldilocks1", "Goldilocks3": "Goldilocks1"}
@@ -70,6 +70,10 @@ def make_job(field, nv, params, npoints, seed, ctx, session=None):
     rng = Rng(seed)
     fid = FIELDS[field]
     vec = field_elements(BASE_OF.get(field, field), params.batch_size << nv, rng=rng)
+    # requests hold their vectors in page-locked memory, so commits upload them by DMA
+    pinned = pinned_empty(vec.size).reshape(vec.shape)
+    pinned[...] = vec
+    vec = pinned
     pts = [field_elements(field, nv, rng=rng).reshape(nv, -1) for _ in range(npoints)]
     vecs = vec.reshape(params.batch_size, 1 << nv, -1)
     evals = [[multilinear_evaluate(ctx, fid, v.reshape(-1), p.reshape(-1)) for v in vecs] for p in pts]
@@ -104,13 +108,14 @@ def prove_jobs_batched(ctx, jobs):
 
 
 class BatchProver:
-    """Proves many jobs over `workers` contexts. With batch_commit, each worker takes a share of the
-    jobs (balanced by size), commits its share at once through commit_batch, then proves them in
-    turn; otherwise every job is committed and proved on its own."""
+    """Proves many jobs over `workers` contexts. With batch_commit, workers take chunks of
+    `commit_group` jobs of similar size, commit each chunk at once through commit_batch, then prove
+    its jobs in turn; otherwise every job is committed and proved on its own."""
 
-    def __init__(self, device=0, workers=8, batch_commit=False):
+    def __init__(self, device=0, workers=8, batch_commit=False, commit_group=4):
         self.contexts = [Context(device) for _ in range(workers)]
         self.batch_commit = batch_commit
+        self.commit_group = max(1, int(commit_group))
 
     def prove_all(self, jobs):
         """Proves every job; returns them in the given order (results in job.narg / job.hints)."""
@@ -145,23 +150,16 @@ class BatchProver:
         return jobs
 
     def _prove_all_batched(self, jobs):
-        # Groups of one embedding and hash engine, split into one chunk per worker of similar total
-        # size (largest job first into the lightest chunk): a worker commits its chunk in shared
-        # launches, then proves its jobs.
+        # Groups of one embedding and hash engine, cut (largest jobs first) into chunks of
+        # `commit_group` jobs of similar size: a worker commits a chunk in shared launches, then
+        # proves its jobs, while other workers commit or prove theirs.
         groups = collections.defaultdict(list)
         for i, j in enumerate(jobs):
             groups[(j.field, bytes(j.params.hash_id))].append(i)
         chunks = []
         for idx in groups.values():
             idx.sort(key=lambda i: -jobs[i].size)
-            nchunks = max(1, min(len(self.contexts), len(idx)))
-            parts = [[] for _ in range(nchunks)]
-            loads = [0] * nchunks
-            for i in idx:
-                k = loads.index(min(loads))
-                parts[k].append(i)
-                loads[k] += jobs[i].size
-            chunks += [p for p in parts if p]
+            chunks += [idx[k:k + self.commit_group] for k in range(0, len(idx), self.commit_group)]
         chunks.sort(key=lambda p: -sum(jobs[i].size for i in p))
         lock = threading.Lock()
         nxt = [0]
