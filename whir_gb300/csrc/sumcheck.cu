@@ -4,13 +4,14 @@
 
 namespace whir {
 
-// Four work items (quads of the fold-and-compute round) per thread: with one item per thread the
-// round kernels' CTAs spent most of their time in the block reduction's barriers (ncu at n = 2^20:
-// 20 % issue-active, barrier stalls first).
-static constexpr size_t SC_ITEMS_PER_THREAD = 4;
+// Work items (quads of the fold-and-compute round) per thread, by size: four at n >= 2^20, where one
+// per thread left the CTAs waiting at the reduction barriers and the last block summing 1024
+// partials (fold-and-compute at 2^20: 45.0 us with one, 27.2 us with four); fewer below, where a
+// small grid leaves the GPU idle (at 2^16: 15.6 us with one against 21.7 us with four).
 size_t sumcheck_partials(size_t n) {
+  const size_t items = n >= (1ull << 20) ? 4 : (n >= (1ull << 18) ? 2 : 1);
   size_t work = std::max<size_t>(n / 4, 1);
-  return std::min(SC_MAX_BLOCKS, (work + SC_THREADS * SC_ITEMS_PER_THREAD - 1) / (SC_THREADS * SC_ITEMS_PER_THREAD));
+  return std::min(SC_MAX_BLOCKS, (work + SC_THREADS * items - 1) / (SC_THREADS * items));
 }
 
 WHIR_SC_INST(Gl)
