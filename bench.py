@@ -41,6 +41,15 @@ FALLBACK_HBM_GBS = 6800.0
 # in proportion to the elements they process, so per-launch traffic = algorithmic bytes x this ratio.
 NCU_TRAFFIC_RATIO = {"encode": (134.601472e6 + 216.216576e6 + 268.512768e6 + 281.217536e6) / 402653184.0}
 
+# The encode kernels are bound by the integer ALU pipe, not HBM. Warp instructions that the commitment
+# encodes of one d=24 proof of this workload issue to the ALU pipe (ncu sm__inst_executed_pipe_alu.sum
+# over the nine encode_cols / encode_rows launches of the four commitments; profiles/
+# ncu_encode_alu_prove_d24_goldilocks2.md), and that pipe's peak issue rate per SM and cycle
+# (sm__inst_executed_pipe_alu.avg.peak_sustained). The count depends on the code and the shapes only,
+# not on the data, so achieved = count / live encode time.
+ENCODE_ALU_WARP_INST = {24: 1034266880}
+ALU_PEAK_WARP_INST_PER_SM_CYCLE = 2.0
+
 
 def parse_args():
     ap = argparse.ArgumentParser()
@@ -57,7 +66,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched / serving measurements")
     ap.add_argument("--batch-jobs", type=int, default=64)
-    ap.add_argument("--serve-jobs", type=int, default=48)
+    ap.add_argument("--serve-jobs", type=int, default=96)
     ap.add_argument("--workers", type=int, default=8,
                     help="worker contexts for the batched / serving runs (8: 914 proofs/s vs 755 with 4)")
     ap.add_argument("--multilimb-nv", type=int, default=20)
@@ -206,30 +215,42 @@ def batched_and_serving(args, dev):
     sref = [(j.narg, j.hints) for j in sjobs]
     capacity = len(sjobs) / cap_s
     rate = 0.7 * capacity
-    srv = serving.ProofServer(dev, workers=args.workers, hbm_budget=150 << 30)
-    t = time.perf_counter()
-    lat = srv.run(sjobs, serving.poisson_arrivals(len(sjobs), rate, seed=6))
-    wall = time.perf_counter() - t
-    srv.close()
-    queue = [j.start - j.arrival for j in sjobs]
-    service = [j.done - j.start for j in sjobs]
-    p99_by_d = {}
-    for d in sorted({j.nv for j in sjobs}):
-        ls = [x for x, j in zip(lat, sjobs) if j.nv == d]
-        p99_by_d[str(d)] = float(np.percentile(ls, 99)) * 1e3
+    arrivals = serving.poisson_arrivals(len(sjobs), rate, seed=6)
+
+    def serve(priority_workers):
+        srv = serving.ProofServer(dev, workers=args.workers, hbm_budget=150 << 30,
+                                  priority_workers=priority_workers, large_nv=22)
+        t = time.perf_counter()
+        lat = srv.run(sjobs, arrivals)
+        wall = time.perf_counter() - t
+        srv.close()
+        queue = [j.start - j.arrival for j in sjobs]
+        service = [j.done - j.start for j in sjobs]
+        p99_by_d = {}
+        for d in sorted({j.nv for j in sjobs}):
+            ls = [x for x, j in zip(lat, sjobs) if j.nv == d]
+            p99_by_d[str(d)] = float(np.percentile(ls, 99)) * 1e3
+        return {
+            "p50_ms": float(np.percentile(lat, 50)) * 1e3, "p99_ms": float(np.percentile(lat, 99)) * 1e3,
+            "queue_p50_ms": float(np.percentile(queue, 50)) * 1e3, "queue_p99_ms": float(np.percentile(queue, 99)) * 1e3,
+            "service_p50_ms": float(np.percentile(service, 50)) * 1e3,
+            "service_p99_ms": float(np.percentile(service, 99)) * 1e3,
+            "p99_by_d_ms": p99_by_d, "proofs_per_s": len(sjobs) / wall,
+            "bit_exact_vs_plain": all((j.narg, j.hints) == r for j, r in zip(sjobs, sref))}
+
+    fifo = serve(0)
+    prio = [serve(k) for k in (2, 4)]
     ctx.close()
     out["serving"] = {
         "workload": "%d requests, Goldilocks2 Blake3 k=4, d uniform over {16,18,20,22,24}, rate 1/2 or 1/4, 1-4 "
-                    "points, unique decoding; Poisson arrivals at 70%% of measured capacity; 150 GB HBM budget"
-                    % len(sjobs),
-        "capacity_proofs_per_s": capacity, "arrival_rate_per_s": rate, "p50_ms": float(np.percentile(lat, 50)) * 1e3,
-        "p99_ms": float(np.percentile(lat, 99)) * 1e3,
-        "queue_p50_ms": float(np.percentile(queue, 50)) * 1e3, "queue_p99_ms": float(np.percentile(queue, 99)) * 1e3,
-        "service_p50_ms": float(np.percentile(service, 50)) * 1e3,
-        "service_p99_ms": float(np.percentile(service, 99)) * 1e3,
-        "p99_by_d_ms": p99_by_d, "proofs_per_s": len(sjobs) / wall, "workers": args.workers,
-        "bit_exact_vs_plain": all((j.narg, j.hints) == r for j, r in zip(sjobs, sref)),
-        "timing": "host wall clock"}
+                    "points, unique decoding; Poisson arrivals at 70%% of measured capacity; 150 GB HBM budget; "
+                    "request vectors in page-locked memory" % len(sjobs),
+        "capacity_proofs_per_s": capacity, "arrival_rate_per_s": rate, **fifo, "workers": args.workers,
+        "policy": "first come first served",
+        "with_priority_workers": [{**r, "policy": "%d of the workers on raised-priority streams take requests of "
+                                                  "d < 22 first, the others larger ones first" % k}
+                                  for k, r in zip((2, 4), prio)],
+        "timing": "host wall clock, the same arrival trace for both policies"}
     return out
 
 
@@ -521,6 +542,22 @@ def run_gpu(args):
     else:
         roofline = {"bound": "integer", "kernel_family": fam, "achieved": None, "peak": peak, "unit": "GB/s",
                     "frac": None, "traffic": None, "avg_launch_ms": ms_f / calls_f}
+    # The bound that sets the encode kernels' time: ALU-pipe issue rate at the SM clock sampled during the
+    # timed region.
+    roofline_alu = None
+    if nv in ENCODE_ALU_WARP_INST and prof.get("encode", (0, 0))[1]:
+        ms_e = prof["encode"][0] / prof_steps
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+        if mhz:
+            ach = ENCODE_ALU_WARP_INST[nv] / (ms_e * 1e-3) / 1e9
+            pk = sms * ALU_PEAK_WARP_INST_PER_SM_CYCLE * mhz * 1e6 / 1e9
+            roofline_alu = {"bound": "alu", "kernel_family": "encode", "achieved": ach, "peak": pk,
+                            "unit": "G warp-inst/s", "frac": ach / pk,
+                            "alu_warp_inst_per_proof": ENCODE_ALU_WARP_INST[nv], "encode_ms_per_proof": ms_e,
+                            "count_source": "ncu count of one proof under the default encode plans",
+                            "peak_source": "%d SMs x %.1f ALU warp-inst/cycle x %.0f MHz sampled SM clock"
+                                           % (sms, ALU_PEAK_WARP_INST_PER_SM_CYCLE, mhz)}
     cpu, bit_exact = None, None
     if not args.no_cpu_baseline:
         cpu, cpu_proof, cpu_nv = cpu_baseline(args)
@@ -538,6 +575,7 @@ def run_gpu(args):
                    "l2": "working set > L2 and a 256 MiB buffer rewritten between steps",
                    "p50_ms": float(np.percentile(times, 50)), "p99_ms": float(np.percentile(times, 99))},
         "roofline": roofline,
+        "roofline_alu": roofline_alu,
         "kernel_families_ms_per_proof": {k: v[0] / prof_steps for k, v in prof.items() if v[1]},
         "autotune": tuned,
         "cpu_baseline": cpu,

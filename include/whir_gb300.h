@@ -71,6 +71,10 @@ const char* whir_last_error(void);
 
 /* ---- context -------------------------------------------------------------------------------- */
 int whir_ctx_create(int device, whir_ctx** out);
+/* A context whose streams have a raised scheduling priority (no reference counterpart): priority 0
+ * is whir_ctx_create's; each step above raises it toward the device's greatest priority. A serving
+ * loop proves its largest requests on such contexts so they are not slowed by the small ones. */
+int whir_ctx_create_priority(int device, int priority, whir_ctx** out);
 int whir_ctx_destroy(whir_ctx* ctx);
 /* Blocks until all work queued on the context's stream has finished. */
 int whir_ctx_synchronize(whir_ctx* ctx);

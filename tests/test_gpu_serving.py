@@ -95,6 +95,19 @@ def test_served_proofs_identical_to_alone(ctx):
         assert j.narg == narg and j.hints == hints, j.session
 
 
+def test_served_proofs_identical_with_priority_workers(ctx):
+    # Small requests on raised-priority contexts, large ones elsewhere: proofs are unchanged.
+    jobs = _small_jobs(ctx, 10, seed=14)
+    ref = _alone(ctx, jobs)
+    srv = serving.ProofServer(device=0, workers=3, hbm_budget=1 << 40, priority_workers=1, large_nv=12)
+    try:
+        srv.run(jobs, serving.poisson_arrivals(len(jobs), 800.0, seed=4))
+    finally:
+        srv.close()
+    for j, (narg, hints) in zip(jobs, ref):
+        assert j.narg == narg and j.hints == hints, j.session
+
+
 def test_server_rejects_request_over_budget(ctx):
     jobs = _small_jobs(ctx, 1, seed=13)
     srv = serving.ProofServer(device=0, workers=1, hbm_budget=1024)

@@ -142,12 +142,13 @@ class ProtocolParameters:
 
 
 class Context:
-    """A CUDA device, its stream and memory pool (one whir_ctx)."""
+    """A CUDA device, its stream and memory pool (one whir_ctx); priority > 0 raises the streams'
+    scheduling priority."""
 
-    def __init__(self, device=0):
+    def __init__(self, device=0, priority=0):
         lib = load_library()
         h = ctypes.c_void_p()
-        _check(lib.whir_ctx_create(ctypes.c_int(device), ctypes.byref(h)))
+        _check(lib.whir_ctx_create_priority(ctypes.c_int(device), ctypes.c_int(priority), ctypes.byref(h)))
         self._h = h
         self.device = device
 

@@ -14,7 +14,7 @@ LIB = os.path.join(HERE, "libwhir_gb300.so")
 SOURCES = ["commit.cu", "commit_mont.cu", "sumcheck.cu", "sumcheck_mont.cu", "prover.cu", "verifier.cu",
            "noalloc.cu"]
 HEADERS = ["field.cuh", "hash.cuh", "kernels.hpp", "protocol.hpp", "status.hpp", "roots.cuh", "encode.cuh",
-           "sumcheck.cuh", "sponge.cuh", "wide.cuh"]
+           "sumcheck.cuh", "sponge.cuh", "wide.cuh", "bulk.cuh"]
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",

@@ -92,10 +92,19 @@ __device__ __forceinline__ B tw_at(const B* tw, int i) {
 // elements at offsets j + k*B/R, k < R, which are exactly the elements those stages combine.
 // Stage st pairs k with k + R/2^(st+1) and multiplies the difference by w_(2h)^(offset mod 2h),
 // 2h = B / 2^st.
-template <class F, int LOGR, bool TWG>
+// LAST marks the final step (B = R, so j = 0): its twiddles are w_(2h)^kk for 2h <= R, the R - 1
+// first table entries, held in registers; the kk = 0 ones are 1 and their products are skipped
+// (7 of the 12 products of a radix-8 step, 3 of 4 for radix 4, all of radix 2).
+template <class F, int LOGR, bool TWG, bool LAST>
 __device__ __forceinline__ void dif_step(F* s, int logn, int logB, int nvec, int lognvec, int vs, int es,
                                          bool vec_fastest, const typename F::Base* tw) {
   constexpr int R = 1 << LOGR;
+  typedef typename F::Base B;
+  B lt[R > 2 ? R - 1 : 1];
+  if constexpr (LAST) {
+#pragma unroll
+    for (int i = 1; i < R - 1; ++i) lt[i] = tw_at<B, TWG>(tw, i);
+  }
   const int logstride = logB - LOGR;
   const int stride = 1 << logstride;
   const int items_log = logn - LOGR;  // work items per vector = n / R
@@ -138,7 +147,11 @@ __device__ __forceinline__ void dif_step(F* s, int logn, int logB, int nvec, int
         const int kk = k & ((1 << (LOGR - st)) - 1);
         const F u = x[k], w = x[k + half];
         x[k] = u + w;
-        x[k + half] = (u - w).mul_base(tw_at<typename F::Base, TWG>(tw, tw0 + kk * stride));
+        if constexpr (LAST) {
+          x[k + half] = kk == 0 ? u - w : (u - w).mul_base(lt[(1 << (LOGR - st - 1)) - 1 + kk]);
+        } else {
+          x[k + half] = (u - w).mul_base(tw_at<B, TWG>(tw, tw0 + kk * stride));
+        }
       }
     }
 #pragma unroll
@@ -155,12 +168,13 @@ __device__ void smem_ntt_dif(F* s, int logn, int nvec, int vs, int es, bool vec_
   int lognvec = 0;
   while ((1 << lognvec) < nvec) ++lognvec;
   int logB = logn;
-  while (logB >= 3) {
-    dif_step<F, 3, TWG>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
+  while (logB > 3) {
+    dif_step<F, 3, TWG, false>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
     logB -= 3;
   }
-  if (logB == 2) dif_step<F, 2, TWG>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
-  if (logB == 1) dif_step<F, 1, TWG>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
+  if (logB == 3) dif_step<F, 3, TWG, true>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
+  if (logB == 2) dif_step<F, 2, TWG, true>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
+  if (logB == 1) dif_step<F, 1, TWG, true>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
 }
 
 // Copies the twiddle levels 1..logn (entries [0, 2^logn - 1)) of the global table into shared memory.
@@ -235,10 +249,30 @@ __device__ __forceinline__ void encode_rows_body(const EncArgs<F>& a, uint64_t b
     const uint64_t C1 = 1ull << a.logC1;
     c_base = bid >> a.logC1;
     k1 = bid & (C1 - 1);
-    #pragma unroll 4
-    for (int idx = threadIdx.x; idx < M * n; idx += blockDim.x) {
-      const int m = idx >> logn, j2 = idx & (n - 1);
-      sts(s, swz<F>(idx), a.src[((((uint64_t)m * a.K + c_base) << a.logC1) + k1) * n + j2]);
+    // Column factor w_N^(j2 (c + K k1)) of the four-step split (see encode_cols_body): one power
+    // per column j2, shared by the M messages; all ones for c = k1 = 0.
+    const uint64_t e = c_base + a.K * k1;
+    const F* src = a.src + (((uint64_t)c_base << a.logC1) + k1) * n;
+    const uint64_t mstride = (a.K << a.logC1) * (uint64_t)n;  // one message's intermediate block
+    if (n >= (int)blockDim.x) {
+      for (int j2 = threadIdx.x; j2 < n; j2 += blockDim.x) {
+        const B f = root_pow<B>(a.rt, a.logN, (e * (uint64_t)j2) & (N - 1));
+        #pragma unroll 4
+        for (int m = 0; m < M; ++m) {
+          F x = src[m * mstride + j2];
+          if (e != 0) x = x.mul_base(f);
+          sts(s, swz<F>((m << logn) + j2), x);
+        }
+      }
+    } else {
+      const int j2 = threadIdx.x & (n - 1);
+      const B f = root_pow<B>(a.rt, a.logN, (e * (uint64_t)j2) & (N - 1));
+      #pragma unroll 4
+      for (int idx = threadIdx.x; idx < M * n; idx += blockDim.x) {
+        F x = src[(idx >> logn) * mstride + j2];
+        if (e != 0) x = x.mul_base(f);
+        sts(s, swz<F>(idx), x);
+      }
     }
   }
   __syncthreads();
@@ -362,70 +396,52 @@ __global__ void __launch_bounds__(ENC_THREADS, EncMinCtas<F>::value) encode_rows
   encode_rows_body<F, KIND>(a, blockIdx.x - jobs[j].cta_begin, smem_raw);
 }
 
-// Four-step pass 1: NTT_C1 over columns j2 of the (C1 x C2) view of each twisted message,
-// multiplied by w_C^(j2 k1); intermediate layout [m][c][k1][j2].
+// w_(2^lvl)^e for e < 2^lvl: from the in-CTA twiddle table (level lvl holds w^q for q < 2^(lvl-1),
+// and w^(q + 2^(lvl-1)) = -w^q) when it has that level, else from the two root tables.
+template <class B>
+__device__ __forceinline__ B level_root(const RootTab& rt, int lvl, uint64_t e) {
+  if (lvl <= NTT_TW_LEVELS) {
+    const uint64_t h = 1ull << (lvl - 1);
+    const B* t = reinterpret_cast<const B*>(rt.ntt) + (h - 1);
+    return e < h ? ldg_elem(t + e) : -ldg_elem(t + (e - h));
+  }
+  return root_pow<B>(rt, lvl, e);
+}
+
+// Four-step pass 1: NTT_C1 over columns j2 of the (C1 x C2) view of each twisted message;
+// intermediate layout [m][c][k1][j2].
+// With j = j1 C2 + j2 and t = k1 + C1 k2 the codeword value is
+//   sum_j2 w_C2^(k2 j2) * w_N^(j2 (c + K k1)) * sum_j1 w_C1^(k1 j1) * w_N^(c j1 C2) * x_j
+// (w_C = w_N^K): this pass applies the row part of the coset twist, w_N^(c j1 C2) = w_(K C1)^(c j1),
+// one table read and one product per element; the factor w_N^(j2 (c + K k1)) depends on j2 only
+// within a row-pass CTA (fixed c, k1), so pass 2 applies it with one power per column shared by
+// all messages.
 template <class F>
 __device__ __forceinline__ void encode_cols_body(const EncArgs<F>& a, uint64_t bid, unsigned char* smem_raw) {
   F* s = reinterpret_cast<F*>(smem_raw);
   const int logn = a.logC1, n = 1 << logn, W = a.W;
+  const int logW = __ffs(W) - 1;  // W is a power of two
   typedef typename F::Base B;
   const B* tw = reinterpret_cast<const B*>(a.rt.ntt);  // read through L1 (keeps shared memory for data)
-  const uint64_t C2 = 1ull << a.logC2, N = 1ull << a.logN;
-  const uint64_t tiles = C2 / W;
+  const uint64_t C2 = 1ull << a.logC2;
+  const uint64_t tiles = C2 >> logW;
   const uint64_t tile = bid % tiles;
   const uint64_t mc = bid / tiles;  // m * K + c
   const uint64_t c = mc % a.K, m = mc / a.K;
-  // With W dividing the block size every thread keeps one column w, and its successive elements
-  // are js = ENC_THREADS / W rows apart: the coset twist w_N^(c j) and the four-step twiddle
-  // w_C^(j2 k1) then advance by a constant factor per element instead of two table reads each.
-  const bool fixed_col = ENC_THREADS % W == 0;
-  const int js = ENC_THREADS / W;
-  if (fixed_col) {
-    const int w = threadIdx.x % W;
-    const uint64_t j2 = tile * W + w;
-    B t = root_pow<B>(a.rt, a.logN, (c * ((((uint64_t)threadIdx.x / W) << a.logC2) + j2)) & (N - 1));
-    const B step = root_pow<B>(a.rt, a.logN, (c * ((uint64_t)js << a.logC2)) & (N - 1));
-    for (int idx = threadIdx.x; idx < n * W; idx += blockDim.x) {
-      const uint64_t j = ((uint64_t)(idx / W) << a.logC2) + j2;
-      F x = j < a.msg_len ? a.src[m * a.msg_len + j] : F::zero();
-      if (c != 0) {
-        x = x.mul_base(t);
-        t = t * step;
-      }
-      sts(s, swz<F>(idx), x);
-    }
-  } else {
-    for (int idx = threadIdx.x; idx < n * W; idx += blockDim.x) {
-      const int j1 = idx / W, w = idx - j1 * W;
-      const uint64_t j = ((uint64_t)j1 << a.logC2) + tile * W + w;
-      F x = j < a.msg_len ? a.src[m * a.msg_len + j] : F::zero();
-      if (c != 0 && j != 0) x = x.mul_base(root_pow<B>(a.rt, a.logN, (c * j) & (N - 1)));
-      sts(s, swz<F>(idx), x);
-    }
+  const int lvl = a.logN - a.logC2;  // log2(K C1)
+  const uint64_t col0 = tile * W;
+  for (int idx = threadIdx.x; idx < n * W; idx += blockDim.x) {
+    const int j1 = idx >> logW;
+    const uint64_t j = ((uint64_t)j1 << a.logC2) + col0 + (idx & (W - 1));
+    F x = j < a.msg_len ? a.src[m * a.msg_len + j] : F::zero();
+    if (c != 0 && j1 != 0) x = x.mul_base(level_root<B>(a.rt, lvl, c * (uint64_t)j1));
+    sts(s, swz<F>(idx), x);
   }
   __syncthreads();
   smem_ntt_dif<F, true>(s, logn, W, 1, W, true, tw);
-  const uint64_t cmask = (1ull << a.logC) - 1;
-  if (fixed_col) {
-    const int w = threadIdx.x % W;
-    const uint64_t j2 = tile * W + w;
-    B t = root_pow<B>(a.rt, a.logC, (j2 * (uint64_t)(threadIdx.x / W)) & cmask);
-    const B step = root_pow<B>(a.rt, a.logC, (j2 * (uint64_t)js) & cmask);
-    for (int idx = threadIdx.x; idx < n * W; idx += blockDim.x) {
-      const int k1 = idx / W;
-      F v = lds(s, swz<F>(brev(k1, logn) * W + w)).mul_base(t);
-      t = t * step;
-      a.dst[((mc << a.logC1) + k1) * C2 + j2] = v;
-    }
-  } else {
-    for (int idx = threadIdx.x; idx < n * W; idx += blockDim.x) {
-      const int k1 = idx / W, w = idx - k1 * W;
-      const uint64_t j2 = tile * W + w;
-      F v = lds(s, swz<F>(brev(k1, logn) * W + w));
-      const uint64_t e = j2 * (uint64_t)k1;
-      if (e) v = v.mul_base(root_pow<B>(a.rt, a.logC, e));
-      a.dst[((mc << a.logC1) + k1) * C2 + j2] = v;
-    }
+  for (int idx = threadIdx.x; idx < n * W; idx += blockDim.x) {
+    const int k1 = idx >> logW, w = idx & (W - 1);
+    a.dst[((mc << a.logC1) + k1) * C2 + col0 + w] = lds(s, swz<F>((brev(k1, logn) << logW) + w));
   }
 }
 

@@ -1052,8 +1052,9 @@ std::vector<T> initial_sumcheck_tensor(whir_ctx* ctx, const Sumcheck& c, Transcr
   const size_t rows = (size_t)1 << sh.R, cols = (size_t)1 << sh.C, per = rows + cols;
   const size_t nz = (size_t)1 << k;
   std::vector<T> rs;
-  DBuf<T> tables(ctx, NF * per), parts(ctx, sh.grid() * NF), out(ctx, nvec * NF * nz);
-  std::vector<T> V(nvec * NF * nz);
+  // out holds the 2^k sums per (vector, form), then an error word (one if a stage wait timed out).
+  DBuf<T> tables(ctx, NF * per), parts(ctx, sh.grid() * NF), out(ctx, nvec * NF * nz + 1);
+  std::vector<T> V(nvec * NF * nz + 1);
   {
     ProfScope prof(ctx, PF_SUMCHECK);
     std::vector<T> ab;
@@ -1071,6 +1072,8 @@ std::vector<T> initial_sumcheck_tensor(whir_ctx* ctx, const Sumcheck& c, Transcr
     }
     CU((launch_tensor_sums<T, S>(x, sh, tables.p, parts.p, out.p, ctx->sc_counter, ctx->stream)));
     d2h(ctx, V.data(), out.p, V.size() * sizeof(T));
+    if (!(V.back() == T::zero())) throw Error(WHIR_ERR_CUDA, "tensor sums: a bulk-copy stage wait timed out");
+    V.pop_back();
   }
   std::vector<T> P(NF, T::one());
   for (int t = 0; t < k; ++t) {
@@ -1609,7 +1612,9 @@ extern "C" {
 
 const char* whir_last_error(void) { return g_last_error.c_str(); }
 
-int whir_ctx_create(int device, whir_ctx** out) {
+int whir_ctx_create(int device, whir_ctx** out) { return whir_ctx_create_priority(device, 0, out); }
+
+int whir_ctx_create_priority(int device, int priority, whir_ctx** out) {
   return guarded([&] {
     if (!out) throw Error(WHIR_ERR_INVALID, "null output pointer");
     int count = 0;
@@ -1622,8 +1627,13 @@ int whir_ctx_create(int device, whir_ctx** out) {
     std::unique_ptr<whir_ctx, int (*)(whir_ctx*)> ctx(new whir_ctx(), whir_ctx_destroy);
     ctx->device = device;
     CU(cudaSetDevice(device));
-    CU(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
-    CU(cudaStreamCreateWithFlags(&ctx->up_stream, cudaStreamNonBlocking));
+    // Stream priority: 0 = the default; a positive value raises it that many steps toward the
+    // device's greatest priority (clamped), so the scheduler runs this context's kernels first.
+    int least = 0, greatest = 0;
+    CU(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    const int prio = std::max(greatest, least - std::max(0, priority));
+    CU(cudaStreamCreateWithPriority(&ctx->stream, cudaStreamNonBlocking, prio));
+    CU(cudaStreamCreateWithPriority(&ctx->up_stream, cudaStreamNonBlocking, prio));
     // Keep freed pool memory cached across proofs.
     cudaMemPool_t pool;
     CU(cudaDeviceGetDefaultMemPool(&pool, device));
@@ -1633,8 +1643,9 @@ int whir_ctx_create(int device, whir_ctx** out) {
     CU(cudaMalloc((void**)&ctx->d_pow, 2 * sizeof(unsigned long long)));
     ctx->sc_parts_bytes = (2 * sumcheck_partials(SIZE_MAX / 64) + 2) * 64;  // max blocks x largest element pair
     CU(cudaMalloc(&ctx->sc_parts, ctx->sc_parts_bytes));
-    CU(cudaMalloc((void**)&ctx->sc_counter, 2 * sizeof(unsigned int)));
-    CU(cudaMemset(ctx->sc_counter, 0, 2 * sizeof(unsigned int)));
+    // (arrival count, launch sequence, error word of the bulk-staged sums, spare)
+    CU(cudaMalloc((void**)&ctx->sc_counter, 4 * sizeof(unsigned int)));
+    CU(cudaMemset(ctx->sc_counter, 0, 4 * sizeof(unsigned int)));
     CU(cudaMalloc((void**)&ctx->geo_counters, GR_MAX_TILES * sizeof(unsigned int)));
     CU(cudaMemset(ctx->geo_counters, 0, GR_MAX_TILES * sizeof(unsigned int)));
     CU(cudaHostAlloc((void**)&ctx->mail_h, MAIL_DATA_OFF + MAIL_DATA_BYTES, cudaHostAllocMapped));

@@ -12,7 +12,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 
+#include "bulk.cuh"
 #include "field.cuh"
 #include "kernels.hpp"
 #include "roots.cuh"
@@ -1000,12 +1002,46 @@ __device__ __forceinline__ void load_cols(const S* p, S* out) {
 // last CTA adds the partials of every (j, f, z) into out[(j nforms + f) 2^k + z]. Rows are read in
 // batches of TS_RB, the next batch's loads issued before the current batch is multiplied (the first
 // version, one column per thread and no prefetch, ran at 16 % of DRAM peak, long-scoreboard bound).
+// Block sums of the per-thread form sums go to partials[blockIdx.x * NF + f]; the last CTA to
+// arrive adds them into out[(j NF + f) 2^k + z], writes out[nout] = 1 if any CTA of the launch
+// recorded an error in counter[2] (else 0) and re-arms counter[0] and counter[2].
+template <class T, int NF>
+__device__ __forceinline__ void tensor_sums_finish(const T (&mine)[NF], const TensorShape& sh, T* partials, T* out,
+                                                   unsigned int* counter) {
+  __shared__ bool am_last;
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    const T s = block_sum(mine[f]);
+    if (threadIdx.x == 0) partials[(uint64_t)blockIdx.x * NF + f] = s;
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    am_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  const uint64_t nz = 1ull << sh.k, groups = sh.row_groups * sh.col_tiles;
+  const uint64_t nout = (uint64_t)sh.nvec * NF * nz;
+  for (uint64_t o = threadIdx.x; o < nout; o += blockDim.x) {
+    const uint64_t zz = o % nz, f = (o / nz) % NF, jj = o / (nz * NF);
+    const T* p = partials + ((jj * nz + zz) * groups) * NF + f;
+    T s = T::zero();
+    for (uint64_t q = 0; q < groups; ++q) s += ldcg_t(p + q * NF);
+    out[o] = s;
+  }
+  if (threadIdx.x == 0) {
+    const unsigned int err = atomicExch(counter + 2, 0u);
+    out[nout] = err ? T::one() : T::zero();
+    counter[0] = 0;
+  }
+}
+
 static constexpr int TS_RB = 4;
 template <class T, class S, int NF, int CPT>
 __global__ void __launch_bounds__(TS_THREADS) tensor_sums_kernel(const S* x, TensorShape sh, const T* tables,
                                                                  T* partials, T* out, unsigned int* counter) {
   __shared__ T srow[NF][TS_MAX_RPC];
-  __shared__ bool am_last;
   const uint64_t rows = 1ull << sh.R, cols = 1ull << sh.C, per = rows + cols;
   uint64_t bid = blockIdx.x;
   const uint64_t tile = bid % sh.col_tiles;
@@ -1072,28 +1108,122 @@ __global__ void __launch_bounds__(TS_THREADS) tensor_sums_kernel(const S* x, Ten
       for (int c = 0; c < CPT; ++c) mine[f] += tables[(uint64_t)f * per + rows + col + c] * acc[f][c].get();
     }
   }
-#pragma unroll
-  for (int f = 0; f < NF; ++f) {
-    const T s = block_sum(mine[f]);
-    if (threadIdx.x == 0) partials[(uint64_t)blockIdx.x * NF + f] = s;
-  }
+  tensor_sums_finish<T, NF>(mine, sh, partials, out, counter);
+}
+
+// Sums pass with the tile staged by the bulk-copy engine: CTA (j, z, row group, 512-column tile)
+// streams its rpc rows of 4 KiB through TB_NST shared-memory stages of TB_RB rows. One thread issues
+// a stage's row copies against the stage's mbarrier; every thread waits for the stage, reads its two
+// columns of each row (one 16-byte shared load) and accumulates; after a CTA barrier the stage is
+// refilled with the rows TB_NST stages ahead. Up to TB_NST x 16 KiB are in flight per CTA with no
+// registers held for them (the register-prefetch version above keeps 64 bytes per thread in flight
+// and runs two CTAs per SM at 100 registers).
+// A stage wait that times out sets the context's error word (counter[2]); the CTA then stops reading,
+// waits (bounded) for its copies still in flight and still takes part in the final reduction, whose
+// last CTA reports the error in out[nout].
+static constexpr int TB_RB = 4;
+static constexpr int TB_NST = 3;
+static constexpr int TB_COLS = 2 * TS_THREADS;
+static constexpr uint32_t TB_ROW_BYTES = TB_COLS * 8;
+static constexpr uint32_t TB_STAGE_BYTES = TB_RB * TB_ROW_BYTES;
+static constexpr size_t TB_SMEM = (size_t)TB_NST * TB_STAGE_BYTES;
+
+// Resident CTAs per SM the bulk kernel is compiled for: its registers are the NF x 2 wide
+// accumulators plus addressing, so more forms or wider fields get fewer CTAs instead of spills.
+template <class T, int NF>
+struct TbMinCtas {
+  static constexpr int value = (NF == 1 && sizeof(T) <= 16) ? 4 : (NF * sizeof(T) <= 32 ? 2 : 1);
+};
+
+template <class T, class S, int NF>
+__global__ void __launch_bounds__(TS_THREADS, TbMinCtas<T, NF>::value) tensor_sums_bulk_kernel(const S* x, TensorShape sh, const T* tables,
+                                                                         T* partials, T* out, unsigned int* counter) {
+  static_assert(sizeof(S) == 8, "two 8-byte source elements per 16-byte shared load");
+  extern __shared__ __align__(128) unsigned char tb_smem[];
+  __shared__ T srow[NF][TS_MAX_RPC];
+  __shared__ __align__(8) uint64_t bar[TB_NST];
+  __shared__ int aborted;
+  const uint64_t rows = 1ull << sh.R, cols = 1ull << sh.C, per = rows + cols;
+  uint64_t bid = blockIdx.x;
+  const uint64_t tile = bid % sh.col_tiles;
+  bid /= sh.col_tiles;
+  const uint64_t g = bid % sh.row_groups;
+  bid /= sh.row_groups;
+  const uint64_t z = bid & ((1ull << sh.k) - 1), j = bid >> sh.k;
+  const uint64_t col0 = tile * TB_COLS, col = col0 + 2 * threadIdx.x;
+  const uint64_t r0 = g * sh.rpc;
+  const S* base = x + j * sh.vec_stride + ((z << sh.R) + r0) * cols + col0;
+  const int nb = sh.rpc / TB_RB;
   if (threadIdx.x == 0) {
-    __threadfence();
-    am_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    aborted = 0;
+#pragma unroll
+    for (int st = 0; st < TB_NST; ++st) mbar_init(&bar[st], 1);
+    mbar_init_fence();
+  }
+  for (int e = threadIdx.x; e < NF * sh.rpc; e += blockDim.x) {
+    const int f = e / sh.rpc, r = e - f * sh.rpc;
+    srow[f][r] = tables[(uint64_t)f * per + r0 + r];
   }
   __syncthreads();
-  if (!am_last) return;
-  __threadfence();
-  const uint64_t nz = 1ull << sh.k, groups = sh.row_groups * sh.col_tiles;
-  const uint64_t nout = (uint64_t)sh.nvec * NF * nz;
-  for (uint64_t o = threadIdx.x; o < nout; o += blockDim.x) {
-    const uint64_t zz = o % nz, f = (o / nz) % NF, jj = o / (nz * NF);
-    const T* p = partials + ((jj * nz + zz) * groups) * NF + f;
-    T s = T::zero();
-    for (uint64_t q = 0; q < groups; ++q) s += ldcg_t(p + q * NF);
-    out[o] = s;
+  auto issue = [&](int b) {
+    const int st = b % TB_NST;
+    unsigned char* dst = tb_smem + (size_t)st * TB_STAGE_BYTES;
+    mbar_arrive_expect_tx(&bar[st], TB_STAGE_BYTES);
+#pragma unroll
+    for (int u = 0; u < TB_RB; ++u)
+      bulk_copy_g2s(dst + u * TB_ROW_BYTES, base + (uint64_t)(b * TB_RB + u) * cols, TB_ROW_BYTES, &bar[st]);
+  };
+  if (threadIdx.x == 0)
+    for (int b = 0; b < nb && b < TB_NST; ++b) issue(b);
+  WideAcc<T> acc[NF][2];
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    acc[f][0].init();
+    acc[f][1].init();
   }
-  if (threadIdx.x == 0) counter[0] = 0;
+  int b = 0;
+  for (; b < nb; ++b) {
+    const int st = b % TB_NST;
+    if (mbar_wait(&bar[st], (uint32_t)(b / TB_NST) & 1)) {
+      const unsigned char* src = tb_smem + (size_t)st * TB_STAGE_BYTES + 16 * threadIdx.x;
+#pragma unroll
+      for (int u = 0; u < TB_RB; ++u) {
+        const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(src + u * TB_ROW_BYTES);
+        S x0, x1;
+        reinterpret_cast<uint64_t*>(&x0)[0] = v.x;
+        reinterpret_cast<uint64_t*>(&x1)[0] = v.y;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          const T w = srow[f][b * TB_RB + u];
+          acc[f][0].mac_mixed(w, x0);
+          acc[f][1].mac_mixed(w, x1);
+        }
+      }
+    } else {
+      aborted = 1;
+    }
+    __syncthreads();
+    if (aborted) break;
+    if (threadIdx.x == 0 && b + TB_NST < nb) {
+      fence_proxy_async_smem();
+      issue(b + TB_NST);
+    }
+  }
+  if (aborted && threadIdx.x == 0) {
+    atomicExch(counter + 2, 1u);
+    // the copies of the stage that timed out and of the stages issued after it
+    for (int q = b; q < nb && q < b + TB_NST; ++q) mbar_wait(&bar[q % TB_NST], (uint32_t)(q / TB_NST) & 1);
+  }
+  T mine[NF];
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    mine[f] = T::zero();
+    if (!aborted) {
+      mine[f] += tables[(uint64_t)f * per + rows + col] * acc[f][0].get();
+      mine[f] += tables[(uint64_t)f * per + rows + col + 1] * acc[f][1].get();
+    }
+  }
+  tensor_sums_finish<T, NF>(mine, sh, partials, out, counter);
 }
 
 // Fold pass: a_out[i] = sum_{j, z} w[j 2^k + z] x_j(z, i) and b_out[i] = sum_f kf[f] row_f[i >> C]
@@ -1147,12 +1277,61 @@ __global__ void tensor_table_kernel(const T* ab, int cnt, T scalar, T* out) {
   }
 }
 
+// Raises a kernel's dynamic shared-memory limit to `bytes` once per device (the flags and results
+// belong to the caller's instantiation).
+static constexpr int SC_MAX_DEVICES = 64;
+template <class K>
+static cudaError_t sc_smem_attr_once(K kernel, size_t bytes, std::once_flag* flags, cudaError_t* results) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= SC_MAX_DEVICES)
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  std::call_once(flags[dev], [&] {
+    results[dev] = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  });
+  return results[dev];
+}
+
+template <class T, class S, int NF>
+static cudaError_t run_tensor_sums_bulk(const S* x, const TensorShape& sh, const T* tables, T* partials, T* out,
+                                        unsigned int* counter, cudaStream_t s) {
+  static std::once_flag flags[SC_MAX_DEVICES];
+  static cudaError_t results[SC_MAX_DEVICES];
+  cudaError_t e = sc_smem_attr_once(tensor_sums_bulk_kernel<T, S, NF>, TB_SMEM, flags, results);
+  if (e != cudaSuccess) return e;
+  tensor_sums_bulk_kernel<T, S, NF><<<(unsigned)sh.grid(), TS_THREADS, TB_SMEM, s>>>(x, sh, tables, partials, out,
+                                                                                     counter);
+  return cudaSuccess;
+}
+
+// The bulk-staged kernel takes full 512-column tiles of 8-byte elements at 16-byte aligned rows.
+inline bool tensor_sums_bulk_ok(const TensorShape& sh, size_t src_bytes) {
+  return sh.cpt == 2 && src_bytes == 8 && sh.threads == TS_THREADS && (1ull << sh.C) % TB_COLS == 0 &&
+         sh.rpc % TB_RB == 0;
+}
+
 template <class T, class S>
 cudaError_t launch_tensor_sums(const S* x, const TensorShape& sh, const T* tables, T* partials, T* out,
                                unsigned int* counter, cudaStream_t s) {
   const unsigned grid = (unsigned)sh.grid();
   const bool two = sh.cpt == 2;
   if (two && (sizeof(S) != 8 || reinterpret_cast<uintptr_t>(x) % 16)) return cudaErrorInvalidValue;
+  if constexpr (sizeof(S) == 8) {
+    if (tensor_sums_bulk_ok(sh, sizeof(S))) {
+      cudaError_t e = cudaSuccess;
+      switch (sh.nforms) {
+        case 1: e = run_tensor_sums_bulk<T, S, 1>(x, sh, tables, partials, out, counter, s); break;
+        case 2: e = run_tensor_sums_bulk<T, S, 2>(x, sh, tables, partials, out, counter, s); break;
+        case 3: e = run_tensor_sums_bulk<T, S, 3>(x, sh, tables, partials, out, counter, s); break;
+        case 4: e = run_tensor_sums_bulk<T, S, 4>(x, sh, tables, partials, out, counter, s); break;
+        default: return cudaErrorInvalidValue;
+      }
+      if (e != cudaSuccess) return e;
+      note_launch();
+      return cudaGetLastError();
+    }
+  }
 #define WHIR_TS_LAUNCH(NF)                                                                                        \
   if (two)                                                                                                        \
     tensor_sums_kernel<T, S, NF, 2><<<grid, sh.threads, 0, s>>>(x, sh, tables, partials, out, counter);          \

@@ -194,10 +194,21 @@ class BatchProver:
 
 
 class ProofServer:
-    """Continuous batching over `workers` contexts with admission by an HBM budget (bytes)."""
+    """Continuous batching over `workers` contexts with admission by an HBM budget (bytes).
 
-    def __init__(self, device=0, workers=8, hbm_budget=150 << 30):
-        self.contexts = [Context(device) for _ in range(workers)]
+    With priority_workers > 0, that many of the workers own contexts with raised stream priority and
+    take the oldest admitted request of fewer than 2^large_nv coefficients first; the other workers
+    take the oldest larger request first. Either falls back to the oldest request of any size. The
+    kernels of small requests then go ahead of the pending blocks of large ones, so a small request's
+    service time stays near its time alone while the large requests absorb the wait."""
+
+    def __init__(self, device=0, workers=8, hbm_budget=150 << 30, priority_workers=0, large_nv=22):
+        priority_workers = max(0, min(priority_workers, workers))
+        self.contexts = [Context(device, priority=1) for _ in range(priority_workers)]
+        self.contexts += [Context(device) for _ in range(workers - priority_workers)]
+        self.prefers_large = [False] * priority_workers + [True] * (workers - priority_workers)
+        self.large_nv = large_nv
+        self.split = priority_workers > 0
         self.budget = hbm_budget
 
     def run(self, jobs, arrivals):
@@ -232,14 +243,23 @@ class ProofServer:
                     admit_locked()
                     cv.notify_all()
 
-        def worker(ctx):
+        def take_locked(large):
+            # oldest admitted request of the preferred size class, else the oldest of any
+            if self.split:
+                for k, i in enumerate(admitted):
+                    if (jobs[i].nv >= self.large_nv) == large:
+                        del admitted[k]
+                        return i
+            return admitted.popleft()
+
+        def worker(ctx, large):
             while True:
                 with cv:
                     while not admitted and state["taken"] < n and state["error"] is None:
                         cv.wait(timeout=0.05)
                     if state["error"] is not None or not admitted:
                         return  # failed elsewhere, or every job has been taken
-                    i = admitted.popleft()
+                    i = take_locked(large)
                     state["taken"] += 1
                     jobs[i].start = time.perf_counter()
                 try:
@@ -255,8 +275,8 @@ class ProofServer:
                     admit_locked()
                     cv.notify_all()
 
-        threads = [threading.Thread(target=feeder)] + [threading.Thread(target=worker, args=(c,))
-                                                       for c in self.contexts]
+        threads = [threading.Thread(target=feeder)] + [threading.Thread(target=worker, args=(c, lg))
+                                                       for c, lg in zip(self.contexts, self.prefers_large)]
         for t in threads:
             t.start()
         for t in threads:
