@@ -47,7 +47,7 @@ NCU_TRAFFIC_RATIO = {"encode": (134.601472e6 + 216.216576e6 + 268.512768e6 + 281
 # ncu_encode_alu_prove_d24_goldilocks2.md), and that pipe's peak issue rate per SM and cycle
 # (sm__inst_executed_pipe_alu.avg.peak_sustained). The count depends on the code and the shapes only,
 # not on the data, so achieved = count / live encode time.
-ENCODE_ALU_WARP_INST = {24: 1034266880}
+ENCODE_ALU_WARP_INST = {24: 924550784}
 ALU_PEAK_WARP_INST_PER_SM_CYCLE = 2.0
 
 

@@ -167,7 +167,17 @@ template <class F, bool TWG>
 __device__ void smem_ntt_dif(F* s, int logn, int nvec, int vs, int es, bool vec_fastest, const typename F::Base* tw) {
   int lognvec = 0;
   while ((1 << lognvec) < nvec) ++lognvec;
+  // The radix-4 / radix-2 remainder goes first, so the last step is radix 8 whenever logn >= 3: its
+  // twiddles are then 5 constant products per 8 elements, and its stride-1 accesses in the column
+  // pass's interleaved layout (element v + i W) stay clear of bank conflicts after the swizzle.
   int logB = logn;
+  if (logB > 3 && logB % 3 == 2) {
+    dif_step<F, 2, TWG, false>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
+    logB -= 2;
+  } else if (logB > 3 && logB % 3 == 1) {
+    dif_step<F, 1, TWG, false>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
+    logB -= 1;
+  }
   while (logB > 3) {
     dif_step<F, 3, TWG, false>(s, logn, logB, nvec, lognvec, vs, es, vec_fastest, tw);
     logB -= 3;
@@ -195,6 +205,12 @@ __device__ __forceinline__ void push_elem_words(const F& x, uint32_t* w) {
   }
 }
 
+// Quotient by the message count through its reciprocal (exact for the tile indices used here: they
+// are below 2^13 and M <= 2^13, so i * M < 2^32); a runtime integer division costs ~20 instructions
+// per element.
+__device__ __forceinline__ int div_m(int i, uint64_t magic) { return (int)(((uint64_t)(uint32_t)i * magic) >> 32); }
+inline uint64_t m_magic_of(uint64_t M) { return M ? ((1ull << 32) + M - 1) / M : 0; }
+
 template <class F>
 struct EncArgs {
   const F* src;  // rows mode 0: messages; rows mode 1: intermediate; cols: messages
@@ -203,6 +219,7 @@ struct EncArgs {
   uint64_t msg_len;
   uint64_t K;  // number of cosets
   int M;       // messages = codeword columns
+  uint64_t m_magic;  // ceil(2^32 / M): i / M = (i * m_magic) >> 32 exactly for i * M < 2^32
   int logC, logN, logC1, logC2;
   int mode;    // rows kernel: 0 single pass, 1 four-step pass 2
   int G;       // cosets per CTA (rows mode 0)
@@ -239,7 +256,7 @@ __device__ __forceinline__ void encode_rows_body(const EncArgs<F>& a, uint64_t b
     #pragma unroll 4
     for (int idx = threadIdx.x; idx < nvec * n; idx += blockDim.x) {
       const int vec = idx >> logn, j = idx & (n - 1);
-      const int g = vec / M, m = vec - g * M;
+      const int g = div_m(vec, a.m_magic), m = vec - g * M;
       const uint64_t c = c_base + g;
       F x = (uint64_t)j < a.msg_len ? a.src[(uint64_t)m * a.msg_len + j] : F::zero();
       if (c != 0 && j != 0) x = x.mul_base(root_pow<B>(a.rt, a.logN, (c * (uint64_t)j) & (N - 1)));
@@ -254,24 +271,36 @@ __device__ __forceinline__ void encode_rows_body(const EncArgs<F>& a, uint64_t b
     const uint64_t e = c_base + a.K * k1;
     const F* src = a.src + (((uint64_t)c_base << a.logC1) + k1) * n;
     const uint64_t mstride = (a.K << a.logC1) * (uint64_t)n;  // one message's intermediate block
-    if (n >= (int)blockDim.x) {
-      for (int j2 = threadIdx.x; j2 < n; j2 += blockDim.x) {
+    // Shared index (m << logn) + j2 with j2 < n: swz of it is swz(j2) ^ swz(m << logn), the second
+    // term the same for every thread.
+    if (n >= ENC_THREADS) {
+      for (int j2 = threadIdx.x; j2 < n; j2 += ENC_THREADS) {
         const B f = root_pow<B>(a.rt, a.logN, (e * (uint64_t)j2) & (N - 1));
+        const int sj = swz<F>(j2);
+        const F* p = src + j2;
         #pragma unroll 4
         for (int m = 0; m < M; ++m) {
-          F x = src[m * mstride + j2];
+          F x = *p;
+          p += mstride;
           if (e != 0) x = x.mul_base(f);
-          sts(s, swz<F>((m << logn) + j2), x);
+          sts(s, sj ^ swz<F>(m << logn), x);
         }
       }
     } else {
+      // idx = threadIdx.x + ENC_THREADS i: column j2 fixed, message advancing by ENC_THREADS / n
       const int j2 = threadIdx.x & (n - 1);
       const B f = root_pow<B>(a.rt, a.logN, (e * (uint64_t)j2) & (N - 1));
+      const int st = swz<F>(threadIdx.x), iters = (M * n + ENC_THREADS - 1) / ENC_THREADS;
+      const F* p = src + (uint64_t)(threadIdx.x >> logn) * mstride + j2;
+      const uint64_t pstep = (uint64_t)(ENC_THREADS >> logn) * mstride;
       #pragma unroll 4
-      for (int idx = threadIdx.x; idx < M * n; idx += blockDim.x) {
-        F x = src[(idx >> logn) * mstride + j2];
-        if (e != 0) x = x.mul_base(f);
-        sts(s, swz<F>(idx), x);
+      for (int i = 0; i < iters; ++i) {
+        if (threadIdx.x + i * ENC_THREADS < M * n) {
+          F x = *p;
+          if (e != 0) x = x.mul_base(f);
+          sts(s, st ^ swz<F>(i * ENC_THREADS), x);
+        }
+        p += pstep;
       }
     }
   }
@@ -279,20 +308,37 @@ __device__ __forceinline__ void encode_rows_body(const EncArgs<F>& a, uint64_t b
   smem_ntt_dif<F, false>(s, logn, nvec, n, 1, false, tw);
 
   // Coalesced row stores: consecutive threads write consecutive columns of consecutive rows.
-  #pragma unroll 4
-  for (int idx = threadIdx.x; idx < R * M; idx += blockDim.x) {
-    const int rho = idx / M, m = idx - rho * M;
-    uint64_t row;
-    int sidx;
-    if (a.mode == 0) {
-      const int g = rho >> logn, t = rho & (n - 1);
-      row = (c_base + g) * C + t;
-      sidx = ((g * M + m) << logn) + brev(t, logn);
-    } else {
-      row = c_base * C + k1 + ((uint64_t)rho << a.logC1);
-      sidx = (m << logn) + brev(rho, logn);
+  const bool m_pow2 = (M & (M - 1)) == 0;
+  if (a.mode == 1 && m_pow2 && M <= ENC_THREADS) {
+    // idx = threadIdx.x + ENC_THREADS i = rho M + m: the column m is fixed per thread and rho advances
+    // by rs = ENC_THREADS / M. brev(rho) = brev(rho0) ^ brev(i rs) (rho0 < rs), so the shared index
+    // (m << logn) + brev(rho) is the thread's first one XOR a term shared by all threads.
+    const int logM = __ffs(M) - 1, m = threadIdx.x & (M - 1), rho0 = threadIdx.x >> logM;
+    const int rs = ENC_THREADS >> logM, iters = (R * M + ENC_THREADS - 1) / ENC_THREADS;
+    const int sb = swz<F>((m << logn) + brev(rho0, logn));
+    F* q = a.dst + (c_base * C + k1 + ((uint64_t)rho0 << a.logC1)) * M + m;
+    const uint64_t qstep = ((uint64_t)rs << a.logC1) * M;
+    #pragma unroll 4
+    for (int i = 0; i < iters; ++i) {
+      if (threadIdx.x + i * ENC_THREADS < R * M) *q = lds(s, sb ^ swz<F>(brev(i * rs, logn)));
+      q += qstep;
     }
-    a.dst[row * M + m] = lds(s, swz<F>(sidx));
+  } else {
+    #pragma unroll 4
+    for (int idx = threadIdx.x; idx < R * M; idx += blockDim.x) {
+      const int rho = div_m(idx, a.m_magic), m = idx - rho * M;
+      uint64_t row;
+      int sidx;
+      if (a.mode == 0) {
+        const int g = rho >> logn, t = rho & (n - 1);
+        row = (c_base + g) * C + t;
+        sidx = ((g * M + m) << logn) + brev(t, logn);
+      } else {
+        row = c_base * C + k1 + ((uint64_t)rho << a.logC1);
+        sidx = (m << logn) + brev(rho, logn);
+      }
+      a.dst[row * M + m] = lds(s, swz<F>(sidx));
+    }
   }
   if (a.leaves == nullptr) return;
   if constexpr (!Canon<F>::IDENTITY) {
@@ -320,6 +366,12 @@ __device__ __forceinline__ void encode_rows_body(const EncArgs<F>& a, uint64_t b
       row = c_base * C + k1 + ((uint64_t)rho << a.logC1);
       base = brev(rho, logn);
     }
+    // Column col of the row sits at base + (col << logn); when that sum has disjoint bit fields
+    // (always in mode 1, where base < n; in mode 0 when M is a power of two) its swizzle is
+    // swz(base) ^ swz(col << logn), the second term shared by all threads.
+    const bool lin = a.mode == 1 || m_pow2;
+    const int sbase = swz<F>(base);
+    auto col_idx = [&](int col) { return lin ? sbase ^ swz<F>(col << logn) : swz<F>(base + (col << logn)); };
     uint32_t out[8];
     if constexpr (KIND == HASH_BLAKE3) {
       // Message blocks assembled in registers (static indices) straight from shared memory:
@@ -335,7 +387,7 @@ __device__ __forceinline__ void encode_rows_body(const EncArgs<F>& a, uint64_t b
           uint64_t limb = 0;
           if (L < limbs) {
             const int col = L / F::LIMBS, part = L - col * F::LIMBS;
-            limb = reinterpret_cast<const uint64_t*>(&s[swz<F>(base + (col << logn))])[part];
+            limb = reinterpret_cast<const uint64_t*>(&s[col_idx(col)])[part];
           }
           mw[2 * q] = (uint32_t)limb;
           mw[2 * q + 1] = (uint32_t)(limb >> 32);
@@ -350,7 +402,7 @@ __device__ __forceinline__ void encode_rows_body(const EncArgs<F>& a, uint64_t b
       h.init((uint32_t)(M * F::LIMBS * 8));
       for (int m = 0; m < M; ++m) {
         uint32_t w[2 * F::LIMBS];
-        push_elem_words<F>(lds(s, swz<F>(base + (m << logn))), w);
+        push_elem_words<F>(lds(s, col_idx(m)), w);
 #pragma unroll
         for (int q = 0; q < 2 * F::LIMBS; ++q) h.push(w[q]);
       }
@@ -430,18 +482,58 @@ __device__ __forceinline__ void encode_cols_body(const EncArgs<F>& a, uint64_t b
   const uint64_t c = mc % a.K, m = mc / a.K;
   const int lvl = a.logN - a.logC2;  // log2(K C1)
   const uint64_t col0 = tile * W;
-  for (int idx = threadIdx.x; idx < n * W; idx += blockDim.x) {
-    const int j1 = idx >> logW;
-    const uint64_t j = ((uint64_t)j1 << a.logC2) + col0 + (idx & (W - 1));
-    F x = j < a.msg_len ? a.src[m * a.msg_len + j] : F::zero();
-    if (c != 0 && j1 != 0) x = x.mul_base(level_root<B>(a.rt, lvl, c * (uint64_t)j1));
-    sts(s, swz<F>(idx), x);
-  }
-  __syncthreads();
-  smem_ntt_dif<F, true>(s, logn, W, 1, W, true, tw);
-  for (int idx = threadIdx.x; idx < n * W; idx += blockDim.x) {
-    const int k1 = idx >> logW, w = idx & (W - 1);
-    a.dst[((mc << a.logC1) + k1) * C2 + col0 + w] = lds(s, swz<F>((brev(k1, logn) << logW) + w));
+  if (W <= ENC_THREADS) {
+    // idx = threadIdx.x + ENC_THREADS i: the thread keeps column w and its row j1 advances by
+    // js = ENC_THREADS / W, so the source and destination addresses advance by fixed strides and the
+    // shared indices are the thread's first ones XOR terms shared by all threads (swz and brev are
+    // linear over GF(2) and the bit fields are disjoint).
+    const int w = threadIdx.x & (W - 1), r0 = threadIdx.x >> logW, js = ENC_THREADS >> logW;
+    const int iters = (n * W + ENC_THREADS - 1) / ENC_THREADS;
+    const bool active = threadIdx.x < n * W;
+    const bool full = a.msg_len >= ((uint64_t)n << a.logC2);  // no zero padding in the message
+    const F* p = a.src + m * a.msg_len + ((uint64_t)r0 << a.logC2) + col0 + w;
+    const uint64_t pstep = (uint64_t)js << a.logC2;
+    const int st = swz<F>(threadIdx.x);
+    if (active) {
+      #pragma unroll 4
+      for (int i = 0; i < iters; ++i) {
+        const int j1 = r0 + i * js;
+        F x;
+        if (full || (((uint64_t)j1 << a.logC2) + col0 + w) < a.msg_len)
+          x = *p;
+        else
+          x = F::zero();
+        if (c != 0 && j1 != 0) x = x.mul_base(level_root<B>(a.rt, lvl, c * (uint64_t)j1));
+        sts(s, st ^ swz<F>(i * ENC_THREADS), x);
+        p += pstep;
+      }
+    }
+    __syncthreads();
+    smem_ntt_dif<F, true>(s, logn, W, 1, W, true, tw);
+    if (active) {
+      const int sb = swz<F>((brev(r0, logn) << logW) + w);
+      F* q = a.dst + ((mc << a.logC1) + r0) * C2 + col0 + w;
+      const uint64_t qstep = (uint64_t)js * C2;
+      #pragma unroll 4
+      for (int i = 0; i < iters; ++i) {
+        *q = lds(s, sb ^ swz<F>(brev(i * js, logn) << logW));
+        q += qstep;
+      }
+    }
+  } else {
+    for (int idx = threadIdx.x; idx < n * W; idx += blockDim.x) {
+      const int j1 = idx >> logW;
+      const uint64_t j = ((uint64_t)j1 << a.logC2) + col0 + (idx & (W - 1));
+      F x = j < a.msg_len ? a.src[m * a.msg_len + j] : F::zero();
+      if (c != 0 && j1 != 0) x = x.mul_base(level_root<B>(a.rt, lvl, c * (uint64_t)j1));
+      sts(s, swz<F>(idx), x);
+    }
+    __syncthreads();
+    smem_ntt_dif<F, true>(s, logn, W, 1, W, true, tw);
+    for (int idx = threadIdx.x; idx < n * W; idx += blockDim.x) {
+      const int k1 = idx >> logW, w = idx & (W - 1);
+      a.dst[((mc << a.logC1) + k1) * C2 + col0 + w] = lds(s, swz<F>((brev(k1, logn) << logW) + w));
+    }
   }
 }
 
@@ -518,6 +610,7 @@ cudaError_t launch_encode(const EncodePlan& p, const F* src, size_t n_msgs, size
   a.leaves = leaves;
   a.msg_len = msg_len;
   a.M = (int)n_msgs;
+  a.m_magic = m_magic_of(n_msgs);
   a.logC = p.logC;
   a.logN = p.logN;
   a.logC1 = p.logC1;
@@ -584,6 +677,7 @@ static EncArgs<F> enc_args_of(const EncodeJobDesc& d, RootTab rt) {
   a.leaves = d.leaves;
   a.msg_len = d.msg_len;
   a.M = (int)d.n_msgs;
+  a.m_magic = m_magic_of(d.n_msgs);
   a.logC = d.plan.logC;
   a.logN = d.plan.logN;
   a.logC1 = d.plan.logC1;

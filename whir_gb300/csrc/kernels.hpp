@@ -313,7 +313,7 @@ cudaError_t launch_tensor_sums(const S* x, const TensorShape& sh, const T* table
                                unsigned int* counter, cudaStream_t s);
 template <class T, class S>
 cudaError_t launch_tensor_fold(const S* x, const TensorShape& sh, const T* w, const T* kf, const T* tables, T* a_out,
-                               T* b_out, cudaStream_t s);
+                               T* b_out, unsigned int* err, cudaStream_t s);
 // out[e] = scalar * prod_q (bit_{cnt-1-q}(e) ? ab[2q+1] : ab[2q]) for e < 2^cnt (device arrays).
 template <class T>
 cudaError_t launch_tensor_table(const T* ab, int cnt, T scalar, T* out, cudaStream_t s);

@@ -229,10 +229,12 @@ void stage_reserve(whir_ctx* ctx, size_t bytes) {
 
 // Copies up to two device segments into the context's host-mapped mail area and then publishes
 // `seq` in the mail flag word (after a system-wide fence), so the host can poll for the data
-// instead of synchronising the stream. One block; 16-, 8- or 1-byte moves by alignment.
+// instead of synchronising the stream. The context's sticky device error word (set by a kernel whose
+// bounded wait timed out) travels in the word after the flag. One block; 16-, 8- or 1-byte moves by
+// alignment.
 __global__ void __launch_bounds__(512) mail_copy_kernel(const uint8_t* s0, size_t b0, const uint8_t* s1, size_t b1,
                                                          uint8_t* dst, size_t off1, unsigned int* flag,
-                                                         unsigned int seq) {
+                                                         unsigned int seq, const unsigned int* dev_err) {
   auto copy = [](const uint8_t* src, size_t bytes, uint8_t* d) {
     const uintptr_t a = reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(d) | bytes;
     if ((a & 15) == 0) {
@@ -247,6 +249,7 @@ __global__ void __launch_bounds__(512) mail_copy_kernel(const uint8_t* s0, size_
   };
   copy(s0, b0, dst);
   if (b1) copy(s1, b1, dst + off1);
+  if (threadIdx.x == 0) reinterpret_cast<volatile unsigned int*>(flag)[1] = *reinterpret_cast<const volatile unsigned int*>(dev_err);
   __threadfence_system();
   __syncthreads();
   if (threadIdx.x == 0) *reinterpret_cast<volatile unsigned int*>(flag) = seq;
@@ -285,7 +288,7 @@ MailFetch mail_begin(whir_ctx* ctx, void* dst0, const void* src0, size_t b0, voi
     mail_copy_kernel<<<1, 512, 0, ctx->stream>>>(static_cast<const uint8_t*>(src0), b0,
                                                  static_cast<const uint8_t*>(src1), b1, ctx->mail_d + MAIL_DATA_OFF,
                                                  f.off1, reinterpret_cast<unsigned int*>(ctx->mail_d + MAIL_FLAG_OFF),
-                                                 f.seq);
+                                                 f.seq, ctx->sc_counter + 3);
     CU(cudaGetLastError());
     note_launch();
   } else {
@@ -314,6 +317,8 @@ void mail_end(whir_ctx* ctx, MailFetch& f) {
         throw Error(WHIR_ERR_CUDA, "timed out waiting for a device result");
     }
   }
+  if (__atomic_load_n(flag_h + 1, __ATOMIC_ACQUIRE) != 0)
+    throw Error(WHIR_ERR_CUDA, "a bounded wait for a bulk copy timed out on the device");
   if (f.b0) memcpy(f.dst0, ctx->mail_h + MAIL_DATA_OFF, f.b0);
   if (f.b1) memcpy(f.dst1, ctx->mail_h + MAIL_DATA_OFF + f.off1, f.b1);
   f.done = true;
@@ -1125,7 +1130,7 @@ std::vector<T> initial_sumcheck_tensor(whir_ctx* ctx, const Sumcheck& c, Transcr
     DBuf<T> dw(ctx, w.size()), dk(ctx, kf.size());
     h2d(ctx, dw.p, w.data(), w.size() * sizeof(T));
     h2d(ctx, dk.p, kf.data(), kf.size() * sizeof(T));
-    CU((launch_tensor_fold<T, S>(x, sh, dw.p, dk.p, tables.p, a, b, ctx->stream)));
+    CU((launch_tensor_fold<T, S>(x, sh, dw.p, dk.p, tables.p, a, b, ctx->sc_counter + 3, ctx->stream)));
   }
   n >>= k;
   return rs;
@@ -1643,7 +1648,8 @@ int whir_ctx_create_priority(int device, int priority, whir_ctx** out) {
     CU(cudaMalloc((void**)&ctx->d_pow, 2 * sizeof(unsigned long long)));
     ctx->sc_parts_bytes = (2 * sumcheck_partials(SIZE_MAX / 64) + 2) * 64;  // max blocks x largest element pair
     CU(cudaMalloc(&ctx->sc_parts, ctx->sc_parts_bytes));
-    // (arrival count, launch sequence, error word of the bulk-staged sums, spare)
+    // (arrival count, launch sequence, error word of the bulk-staged sums, sticky device error word
+    // that every mail publication carries to the host)
     CU(cudaMalloc((void**)&ctx->sc_counter, 4 * sizeof(unsigned int)));
     CU(cudaMemset(ctx->sc_counter, 0, 4 * sizeof(unsigned int)));
     CU(cudaMalloc((void**)&ctx->geo_counters, GR_MAX_TILES * sizeof(unsigned int)));

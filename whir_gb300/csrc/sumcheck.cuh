@@ -1211,6 +1211,7 @@ __global__ void __launch_bounds__(TS_THREADS, TbMinCtas<T, NF>::value) tensor_su
   }
   if (aborted && threadIdx.x == 0) {
     atomicExch(counter + 2, 1u);
+    atomicExch(counter + 3, 1u);
     // the copies of the stage that timed out and of the stages issued after it
     for (int q = b; q < nb && q < b + TB_NST; ++q) mbar_wait(&bar[q % TB_NST], (uint32_t)(q / TB_NST) & 1);
   }
@@ -1264,6 +1265,100 @@ __global__ void __launch_bounds__(TS_THREADS) tensor_fold_kernel(const S* x, Ten
     }
     b_out[i] = bv;
   }
+}
+
+// Fold pass with the source rows staged by the bulk-copy engine (8-byte sources, 512-output tiles):
+// CTA = outputs [i0, i0 + 512); its nvec 2^k source rows x_j(z, i0 .. i0 + 511) (4 KiB each) stream
+// through TB_NST shared-memory stages of TB_RB rows as in the sums pass, each thread accumulating
+// two adjacent outputs. Waits are bounded as in tensor_sums_bulk_kernel; a timeout sets the error
+// word counter[2], which the host reads back after the fold.
+// Issues stage q % TB_NST of the fold: rows r = q TB_RB + u, row r = (vector r >> nz_log, z = the low
+// bits), each TB_ROW_BYTES from x_j(z, i0).
+template <class S>
+__device__ __forceinline__ void fold_issue(unsigned char* smem, uint64_t* bar, int q, const S* xt, uint64_t vstride,
+                                           uint64_t len, int nz_log) {
+  const int st = q % TB_NST;
+  unsigned char* dst = smem + (size_t)st * TB_STAGE_BYTES;
+  mbar_arrive_expect_tx(&bar[st], TB_STAGE_BYTES);
+#pragma unroll
+  for (int u = 0; u < TB_RB; ++u) {
+    const int r = q * TB_RB + u, j = r >> nz_log, z = r & ((1 << nz_log) - 1);
+    bulk_copy_g2s(dst + u * TB_ROW_BYTES, xt + (uint64_t)j * vstride + (uint64_t)z * len, TB_ROW_BYTES, &bar[st]);
+  }
+}
+
+template <class T, class S>
+__global__ void __launch_bounds__(TS_THREADS, sizeof(T) <= 8 ? 4 : (sizeof(T) <= 16 ? 3 : 2)) tensor_fold_bulk_kernel(const S* x, TensorShape sh, const T* w,
+                                                                        const T* kf, const T* tables, T* a_out,
+                                                                        T* b_out, unsigned int* err) {
+  static_assert(sizeof(S) == 8, "two 8-byte source elements per 16-byte shared load");
+  extern __shared__ __align__(128) unsigned char tb_smem[];
+  __shared__ __align__(8) uint64_t bar[TB_NST];
+  __shared__ int aborted;
+  const uint64_t rows = 1ull << sh.R, cols = 1ull << sh.C, per = rows + cols, len = rows * cols;
+  const int nz_log = sh.k, nrows = sh.nvec << sh.k, nb = nrows / TB_RB;
+  T* sw = reinterpret_cast<T*>(tb_smem + TB_SMEM);  // the nrows fold weights after the stages
+  const uint64_t i0 = (uint64_t)blockIdx.x * TB_COLS;
+  if (threadIdx.x == 0) {
+    aborted = 0;
+#pragma unroll
+    for (int st = 0; st < TB_NST; ++st) mbar_init(&bar[st], 1);
+    mbar_init_fence();
+  }
+  for (int e = threadIdx.x; e < nrows; e += blockDim.x) sw[e] = w[e];
+  __syncthreads();
+  const S* xt = x + i0;
+  const uint64_t vstride = sh.vec_stride;
+  if (threadIdx.x == 0)
+    for (int q = 0; q < nb && q < TB_NST; ++q) fold_issue<S>(tb_smem, bar, q, xt, vstride, len, nz_log);
+  WideAcc<T> acc0, acc1;
+  acc0.init();
+  acc1.init();
+  int b = 0;
+  for (; b < nb; ++b) {
+    const int st = b % TB_NST;
+    if (mbar_wait(&bar[st], (uint32_t)(b / TB_NST) & 1)) {
+      const unsigned char* src = tb_smem + (size_t)st * TB_STAGE_BYTES + 16 * threadIdx.x;
+#pragma unroll
+      for (int u = 0; u < TB_RB; ++u) {
+        const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(src + u * TB_ROW_BYTES);
+        S x0, x1;
+        reinterpret_cast<uint64_t*>(&x0)[0] = v.x;
+        reinterpret_cast<uint64_t*>(&x1)[0] = v.y;
+        const T wr = sw[b * TB_RB + u];
+        acc0.mac_mixed(wr, x0);
+        acc1.mac_mixed(wr, x1);
+      }
+    } else {
+      aborted = 1;
+    }
+    __syncthreads();
+    if (aborted) break;
+    if (threadIdx.x == 0 && b + TB_NST < nb) {
+      fence_proxy_async_smem();
+      fold_issue<S>(tb_smem, bar, b + TB_NST, xt, vstride, len, nz_log);
+    }
+  }
+  if (aborted) {
+    if (threadIdx.x == 0) {
+      atomicExch(err, 1u);
+      for (int q = b; q < nb && q < b + TB_NST; ++q) mbar_wait(&bar[q % TB_NST], (uint32_t)(q / TB_NST) & 1);
+    }
+    return;
+  }
+  const uint64_t i = i0 + 2 * threadIdx.x;
+  a_out[i] = acc0.get();
+  a_out[i + 1] = acc1.get();
+  const uint64_t H = i >> sh.C, c = i & (cols - 1);  // i and i + 1 share the row (cols >= 2)
+  T b0 = T::zero(), b1 = T::zero();
+  for (int f = 0; f < sh.nforms; ++f) {
+    const T* tf = tables + (uint64_t)f * per;
+    const T rowk = kf[f] * tf[H];
+    b0 += rowk * tf[rows + c];
+    b1 += rowk * tf[rows + c + 1];
+  }
+  b_out[i] = b0;
+  b_out[i + 1] = b1;
 }
 
 // Tensor table of `cnt` variables: out[e] = scalar * prod_q (bit_{cnt-1-q}(e) ? ab[2q+1] : ab[2q]).
@@ -1350,11 +1445,35 @@ cudaError_t launch_tensor_sums(const S* x, const TensorShape& sh, const T* table
 }
 
 template <class T, class S>
+static cudaError_t run_tensor_fold_bulk(const S* x, const TensorShape& sh, const T* w, const T* kf, const T* tables,
+                                        T* a_out, T* b_out, unsigned int* err, cudaStream_t s) {
+  static std::once_flag flags[SC_MAX_DEVICES];
+  static cudaError_t results[SC_MAX_DEVICES];
+  const size_t smem = TB_SMEM + ((size_t)sh.nvec << sh.k) * sizeof(T);
+  cudaError_t e = sc_smem_attr_once(tensor_fold_bulk_kernel<T, S>, TB_SMEM + 48 * 1024, flags, results);
+  if (e != cudaSuccess) return e;
+  const uint64_t len = 1ull << (sh.R + sh.C);
+  tensor_fold_bulk_kernel<T, S><<<(unsigned)(len / TB_COLS), TS_THREADS, smem, s>>>(x, sh, w, kf, tables, a_out, b_out,
+                                                                                  err);
+  return cudaSuccess;
+}
+
+template <class T, class S>
 cudaError_t launch_tensor_fold(const S* x, const TensorShape& sh, const T* w, const T* kf, const T* tables, T* a_out,
-                               T* b_out, cudaStream_t s) {
+                               T* b_out, unsigned int* err, cudaStream_t s) {
   const uint64_t len = 1ull << (sh.R + sh.C);
   const size_t smem = ((size_t)sh.nvec << sh.k) * sizeof(T);
   if (smem > 48 * 1024) return cudaErrorInvalidValue;
+  if constexpr (sizeof(S) == 8) {
+    // bulk-staged: whole 512-output tiles, 16-byte aligned rows, whole stages of rows
+    if (err && len % TB_COLS == 0 && reinterpret_cast<uintptr_t>(x) % 16 == 0 && sh.vec_stride % 2 == 0 &&
+        ((sh.nvec << sh.k) % TB_RB) == 0 && (1ull << sh.C) >= 2) {
+      cudaError_t e = run_tensor_fold_bulk<T, S>(x, sh, w, kf, tables, a_out, b_out, err, s);
+      if (e != cudaSuccess) return e;
+      note_launch();
+      return cudaGetLastError();
+    }
+  }
   const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((len + TS_THREADS - 1) / TS_THREADS,
                                                                            SC_MAX_BLOCKS * 4));
   tensor_fold_kernel<T, S><<<grid, TS_THREADS, smem, s>>>(x, sh, w, kf, tables, a_out, b_out);
@@ -1483,6 +1602,6 @@ cudaError_t launch_univariate_eval(const S* coeffs, size_t n, T x, T* partials, 
   template cudaError_t launch_tensor_sums<T, S>(const S*, const TensorShape&, const T*, T*, T*, unsigned int*,     \
                                                 cudaStream_t);                                                   \
   template cudaError_t launch_tensor_fold<T, S>(const S*, const TensorShape&, const T*, const T*, const T*, T*, T*, \
-                                                cudaStream_t);
+                                                unsigned int*, cudaStream_t);
 
 }  // namespace whir
