@@ -288,10 +288,23 @@ __device__ __forceinline__ void merkle_tile_body(uint32_t* nodes, int layers, in
   }
 }
 
+// Copies a result that this CTA has written to global memory into a mail slot and publishes it
+// (call after a CTA barrier, from one thread).
+__device__ __forceinline__ void mail_publish(const MailSlot& mail, const uint32_t* src, int words) {
+  for (int i = 0; i < words; ++i) reinterpret_cast<volatile uint32_t*>(mail.data)[i] = src[i];
+  reinterpret_cast<volatile unsigned int*>(mail.flag)[1] = *reinterpret_cast<const volatile unsigned int*>(mail.dev_err);
+  __threadfence_system();
+  *reinterpret_cast<volatile unsigned int*>(mail.flag) = mail.seq;
+}
+
 template <int KIND, int S>
 __global__ void __launch_bounds__(MK_THREADS) merkle_tile_kernel(uint32_t* nodes, int layers, int in_level,
-                                                                 int nlev) {
+                                                                 int nlev, MailSlot mail) {
   merkle_tile_body<KIND, S>(nodes, layers, in_level, nlev, blockIdx.x);
+  if (mail.data == nullptr) return;
+  // the single CTA of the top tile: the root is the tree's last node
+  __syncthreads();
+  if (threadIdx.x == 0) mail_publish(mail, nodes + ((2ull << layers) - 2) * 8, 8);
 }
 
 // Several trees in one launch per tile step: tree j's tiles are CTAs [cta_begin_j, cta_begin_j+1).
@@ -378,17 +391,19 @@ cudaError_t launch_merkle_multi(const std::vector<MerkleMultiLaunch>& launches, 
 }
 
 template <int KIND>
-static cudaError_t merkle_run(uint32_t* nodes, int layers, cudaStream_t s, int tile_log) {
+static cudaError_t merkle_run(uint32_t* nodes, int layers, cudaStream_t s, int tile_log, const MailSlot& mail) {
   tile_log = std::max(1, std::min(tile_log, MK_MAX_TILE_LOG));
+  if (mail.data && layers < 1) return cudaErrorInvalidValue;
   int level = 0;
   while (level < layers) {
     const int nlev = std::min(tile_log, layers - level);
     const int S = std::max(0, nlev - 8);
     const unsigned grid = (unsigned)((1ull << (layers - level)) >> nlev);
+    const MailSlot m = level + nlev == layers ? mail : MailSlot();  // the last launch is one CTA
     switch (S) {
-      case 0: merkle_tile_kernel<KIND, 0><<<grid, MK_THREADS, 0, s>>>(nodes, layers, level, nlev); break;
-      case 1: merkle_tile_kernel<KIND, 1><<<grid, MK_THREADS, 0, s>>>(nodes, layers, level, nlev); break;
-      default: merkle_tile_kernel<KIND, 2><<<grid, MK_THREADS, 0, s>>>(nodes, layers, level, nlev); break;
+      case 0: merkle_tile_kernel<KIND, 0><<<grid, MK_THREADS, 0, s>>>(nodes, layers, level, nlev, m); break;
+      case 1: merkle_tile_kernel<KIND, 1><<<grid, MK_THREADS, 0, s>>>(nodes, layers, level, nlev, m); break;
+      default: merkle_tile_kernel<KIND, 2><<<grid, MK_THREADS, 0, s>>>(nodes, layers, level, nlev, m); break;
     }
     note_launch();
     cudaError_t e = cudaGetLastError();
@@ -398,13 +413,13 @@ static cudaError_t merkle_run(uint32_t* nodes, int layers, cudaStream_t s, int t
   return cudaSuccess;
 }
 
-cudaError_t launch_merkle(uint32_t* nodes, int layers, int kind, cudaStream_t s, int tile_log) {
+cudaError_t launch_merkle(uint32_t* nodes, int layers, int kind, cudaStream_t s, int tile_log, const MailSlot& mail) {
   if (tile_log <= 0) tile_log = merkle_tile_log_for(layers);
   switch (kind) {
-    case HASH_BLAKE3: return merkle_run<HASH_BLAKE3>(nodes, layers, s, tile_log);
-    case HASH_SHA2: return merkle_run<HASH_SHA2>(nodes, layers, s, tile_log);
-    case HASH_SHA3: return merkle_run<HASH_SHA3>(nodes, layers, s, tile_log);
-    case HASH_KECCAK: return merkle_run<HASH_KECCAK>(nodes, layers, s, tile_log);
+    case HASH_BLAKE3: return merkle_run<HASH_BLAKE3>(nodes, layers, s, tile_log, mail);
+    case HASH_SHA2: return merkle_run<HASH_SHA2>(nodes, layers, s, tile_log, mail);
+    case HASH_SHA3: return merkle_run<HASH_SHA3>(nodes, layers, s, tile_log, mail);
+    case HASH_KECCAK: return merkle_run<HASH_KECCAK>(nodes, layers, s, tile_log, mail);
     default: return cudaErrorInvalidValue;  // Copy cannot hash 64-byte nodes
   }
 }
@@ -448,66 +463,62 @@ struct PowArgs {
   uint32_t chal[8];
   uint32_t pre[16];  // Blake3: state after the nonce-independent part of round 1 (blake3_pow_prefix)
   uint64_t threshold, start, count;
-  unsigned long long* best;
-  unsigned long long* counter;
+  unsigned long long* best;  // best[0]: lowest hit so far; best[1]: finished CTAs
+  MailSlot mail;
 };
 
 static constexpr int POW_THREADS = 256;
-static constexpr int POW_PER_THREAD = 4;
-static constexpr uint64_t POW_BLOCK = (uint64_t)POW_THREADS * POW_PER_THREAD;
 
-// CTAs claim consecutive blocks of POW_BLOCK nonces in increasing order and stop at the first block
-// that starts at or above the best nonce found so far. Every block below the final best has been
-// searched completely, so the result is the lowest satisfying nonce of the range.
+// Thread t of the grid (T threads) tries nonces start + t, start + t + T, start + t + 2T, ... and
+// stops at the first one at or above the best nonce known so far; a satisfying nonce lowers the best
+// with atomicMin. Every nonce below the final best is tried by its thread, so the result is the
+// lowest satisfying nonce of the range. The grid is one wave of resident CTAs, so the threads advance
+// together and, once a hit is known, each does at most the hash in progress (no block claims, no
+// barriers). The best nonce is re-read before every hash and the read of one iteration is used by the
+// next, so its latency hides behind a hash.
 template <int KIND>
 __global__ void __launch_bounds__(POW_THREADS) pow_kernel(PowArgs a) {
-  __shared__ unsigned long long s_start;
-  for (;;) {
-    if (threadIdx.x == 0) {
-      const unsigned long long b = atomicAdd(a.counter, 1ull);
-      const unsigned long long off = b * POW_BLOCK;
-      const unsigned long long st = a.start + off;
-      const unsigned long long best = *reinterpret_cast<volatile unsigned long long*>(a.best);
-      s_start = (off >= a.count || st >= best) ? ~0ull : st;
-    }
-    __syncthreads();
-    const unsigned long long st = s_start;
-    __syncthreads();
-    if (st == ~0ull) return;
-    // The best nonce so far is re-read before every hash (the read of one iteration is used by the
-    // next, so its latency hides behind a hash): once a satisfying nonce at or below this thread's
-    // next nonce is known, the rest of the block cannot lower the result and is skipped. Without
-    // this, every block claimed before the first hit ran to completion (about one full wave of
-    // nonces beyond the answer).
-    unsigned long long known = *reinterpret_cast<volatile unsigned long long*>(a.best);
+  const uint64_t T = (uint64_t)gridDim.x * blockDim.x;
+  unsigned long long known = *reinterpret_cast<volatile unsigned long long*>(a.best);
 #pragma unroll 1
-    for (int q = 0; q < POW_PER_THREAD; ++q) {
-      const uint64_t off = (uint64_t)q * POW_THREADS + threadIdx.x;
-      if (st - a.start + off >= a.count) break;
-      const uint64_t nonce = st + off;
-      if (nonce >= known) break;
-      known = *reinterpret_cast<volatile unsigned long long*>(a.best);
-      uint32_t h[8];
-      if constexpr (KIND == HASH_BLAKE3) {
-        blake3_pow_tail(a.pre, a.chal, (uint32_t)nonce, (uint32_t)(nonce >> 32), h[0], h[1]);
-      } else {
-        uint32_t m[16];
+  for (uint64_t off = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; off < a.count; off += T) {
+    const uint64_t nonce = a.start + off;
+    if (nonce >= known) break;
+    known = *reinterpret_cast<volatile unsigned long long*>(a.best);
+    uint32_t h[8];
+    if constexpr (KIND == HASH_BLAKE3) {
+      blake3_pow_tail(a.pre, a.chal, (uint32_t)nonce, (uint32_t)(nonce >> 32), h[0], h[1]);
+    } else {
+      uint32_t m[16];
 #pragma unroll
-        for (int w = 0; w < 8; ++w) m[w] = a.chal[w];
-        m[8] = (uint32_t)nonce;
-        m[9] = (uint32_t)(nonce >> 32);
+      for (int w = 0; w < 8; ++w) m[w] = a.chal[w];
+      m[8] = (uint32_t)nonce;
+      m[9] = (uint32_t)(nonce >> 32);
 #pragma unroll
-        for (int w = 10; w < 16; ++w) m[w] = 0;
-        hash64<KIND>(m, h);
-      }
-      const uint64_t v = (uint64_t)h[0] | ((uint64_t)h[1] << 32);
-      if (v <= a.threshold) atomicMin(a.best, (unsigned long long)nonce);
+      for (int w = 10; w < 16; ++w) m[w] = 0;
+      hash64<KIND>(m, h);
+    }
+    const uint64_t v = (uint64_t)h[0] | ((uint64_t)h[1] << 32);
+    if (v <= a.threshold) atomicMin(a.best, (unsigned long long)nonce);
+  }
+  if (a.mail.data == nullptr) return;
+  // The last CTA to finish publishes the result (every CTA's atomicMin precedes its arrival).
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(a.best + 1, 1ull) == gridDim.x - 1) {
+      const unsigned long long b = *reinterpret_cast<volatile unsigned long long*>(a.best);
+      *reinterpret_cast<volatile unsigned long long*>(a.mail.data) = b;
+      reinterpret_cast<volatile unsigned int*>(a.mail.flag)[1] =
+          *reinterpret_cast<const volatile unsigned int*>(a.mail.dev_err);
+      __threadfence_system();
+      *reinterpret_cast<volatile unsigned int*>(a.mail.flag) = a.mail.seq;
     }
   }
 }
 
 cudaError_t launch_pow(const uint32_t challenge[8], uint64_t threshold, uint64_t start, uint64_t count,
-                       unsigned long long* best, int kind, cudaStream_t s) {
+                       unsigned long long* best, int kind, cudaStream_t s, const MailSlot& mail) {
   PowArgs a;
   for (int i = 0; i < 8; ++i) a.chal[i] = challenge[i];
   blake3_pow_prefix(a.chal, a.pre);
@@ -515,15 +526,42 @@ cudaError_t launch_pow(const uint32_t challenge[8], uint64_t threshold, uint64_t
   a.start = start;
   a.count = count;
   a.best = best;
-  a.counter = best + 1;  // the caller provides two words: best nonce, block counter (both reset)
-  unsigned grid = (unsigned)std::min<uint64_t>((count + POW_BLOCK - 1) / POW_BLOCK, 152ull * 8);
+  a.mail = mail;
+  // The grid is exactly the CTAs that fit on the GPU at once (by the kernel's registers), so every
+  // thread starts at once; a larger grid would hold CTAs back until the first ones exit.
+  auto resident = [&](auto kernel) -> unsigned {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+        cudaSuccess || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, POW_THREADS, 0) != cudaSuccess ||
+        per_sm < 1 || sms < 1)
+      return 152;
+    return (unsigned)(sms * per_sm);
+  };
+  const uint64_t want = (count + POW_THREADS - 1) / POW_THREADS;
   switch (kind) {
-    case HASH_BLAKE3: pow_kernel<HASH_BLAKE3><<<grid, 256, 0, s>>>(a); note_launch(); break;
-    case HASH_SHA2: pow_kernel<HASH_SHA2><<<grid, 256, 0, s>>>(a); note_launch(); break;
-    case HASH_SHA3: pow_kernel<HASH_SHA3><<<grid, 256, 0, s>>>(a); note_launch(); break;
-    case HASH_KECCAK: pow_kernel<HASH_KECCAK><<<grid, 256, 0, s>>>(a); note_launch(); break;
+    case HASH_BLAKE3: {
+      static const unsigned r = resident(pow_kernel<HASH_BLAKE3>);
+      pow_kernel<HASH_BLAKE3><<<(unsigned)std::min<uint64_t>(want, r), POW_THREADS, 0, s>>>(a);
+      break;
+    }
+    case HASH_SHA2: {
+      static const unsigned r = resident(pow_kernel<HASH_SHA2>);
+      pow_kernel<HASH_SHA2><<<(unsigned)std::min<uint64_t>(want, r), POW_THREADS, 0, s>>>(a);
+      break;
+    }
+    case HASH_SHA3: {
+      static const unsigned r = resident(pow_kernel<HASH_SHA3>);
+      pow_kernel<HASH_SHA3><<<(unsigned)std::min<uint64_t>(want, r), POW_THREADS, 0, s>>>(a);
+      break;
+    }
+    case HASH_KECCAK: {
+      static const unsigned r = resident(pow_kernel<HASH_KECCAK>);
+      pow_kernel<HASH_KECCAK><<<(unsigned)std::min<uint64_t>(want, r), POW_THREADS, 0, s>>>(a);
+      break;
+    }
     default: return cudaErrorInvalidValue;
   }
+  note_launch();
   return cudaGetLastError();
 }
 

@@ -664,6 +664,60 @@ cudaError_t launch_encode(const EncodePlan& p, const F* src, size_t n_msgs, size
   return dispatch_rows<F>(a, hash_kind, (unsigned)(a.K * C1), smem, s);
 }
 
+// Pass 1 of the four-step split for one message of one coset (K = 1) given by its nonzero
+// coefficients grouped by column j2: CTA q writes the whole intermediate column
+// I[k1][j2] = sum_e val_e w_C1^(k1 j1_e), k1 < C1, for j2 = col_j2[q] and entries
+// [col_off[q], col_off[q + 1]); the caller zeroes the intermediate first (its other columns are zero).
+template <class F>
+__global__ void sparse_cols_kernel(const uint32_t* col_j2, const uint32_t* col_off, const uint32_t* ent_j1,
+                                   const F* ent_val, int logC1, int logC2, RootTab rt, F* inter) {
+  typedef typename F::Base B;
+  const uint32_t j2 = col_j2[blockIdx.x], e0 = col_off[blockIdx.x], e1 = col_off[blockIdx.x + 1];
+  const uint64_t C1 = 1ull << logC1;
+  for (uint64_t k1 = threadIdx.x; k1 < C1; k1 += blockDim.x) {
+    F acc = F::zero();
+    for (uint32_t e = e0; e < e1; ++e) acc += ent_val[e].mul_base(level_root<B>(rt, logC1, (k1 * ent_j1[e]) & (C1 - 1)));
+    inter[(k1 << logC2) + j2] = acc;
+  }
+}
+
+template <class F>
+cudaError_t launch_sparse_cols(const EncodePlan& p, const uint32_t* col_j2, const uint32_t* col_off,
+                               const uint32_t* ent_j1, const F* ent_val, size_t ncols, F* inter, RootTab rt,
+                               cudaStream_t s) {
+  if (p.mode != 1 || p.logN != p.logC || p.logC1 < 1 || ncols == 0) return cudaErrorInvalidValue;
+  sparse_cols_kernel<F><<<(unsigned)ncols, 256, 0, s>>>(col_j2, col_off, ent_j1, ent_val, p.logC1, p.logC2, rt, inter);
+  note_launch();
+  return cudaGetLastError();
+}
+
+// Pass 2 alone (the four-step row pass) of an encode whose intermediate `scratch` was produced
+// elsewhere (launch_sparse_cols); no leaf hashing.
+template <class F>
+cudaError_t launch_encode_rows_pass(const EncodePlan& p, const F* scratch, size_t n_msgs, size_t msg_len, F* dst,
+                                    RootTab rt, cudaStream_t s) {
+  if (p.mode != 1 || p.logN > rt.log_order || p.logN > 32) return cudaErrorInvalidValue;
+  EncArgs<F> a;
+  a.leaves = nullptr;
+  a.msg_len = msg_len;
+  a.M = (int)n_msgs;
+  a.m_magic = m_magic_of(n_msgs);
+  a.logC = p.logC;
+  a.logN = p.logN;
+  a.logC1 = p.logC1;
+  a.logC2 = p.logC2;
+  a.K = 1ull << (p.logN - p.logC);
+  a.G = p.cosets_per_cta;
+  a.W = p.cols_per_cta;
+  a.rt = rt;
+  a.mode = 1;
+  a.src = scratch;
+  a.dst = dst;
+  const size_t C1 = 1ull << p.logC1, C2 = 1ull << p.logC2;
+  const size_t smem = n_msgs * C2 * sizeof(F) + C2 * sizeof(typename F::Base) + 16;
+  return dispatch_rows<F>(a, HASH_COPY, (unsigned)(a.K * C1), smem, s);
+}
+
 // Multi-job encode: the host image holds the column-pass table then (16-byte aligned) the row-pass
 // table, one EncJob per job with the CTA index its range starts at.
 template <class F>
@@ -840,6 +894,10 @@ cudaError_t launch_to_canonical(F* v, size_t n, cudaStream_t s) {
   template cudaError_t launch_encode_multi<F>(const EncodeMultiLaunch&, const void*, int, cudaStream_t);         \
   template cudaError_t launch_gather_rows<F>(const F*, size_t, const uint64_t*, size_t, F*, cudaStream_t);       \
   template cudaError_t launch_to_internal<F>(F*, size_t, cudaStream_t);                                         \
-  template cudaError_t launch_to_canonical<F>(F*, size_t, cudaStream_t);
+  template cudaError_t launch_to_canonical<F>(F*, size_t, cudaStream_t);                                         \
+  template cudaError_t launch_sparse_cols<F>(const EncodePlan&, const uint32_t*, const uint32_t*, const uint32_t*,  \
+                                             const F*, size_t, F*, RootTab, cudaStream_t);                        \
+  template cudaError_t launch_encode_rows_pass<F>(const EncodePlan&, const F*, size_t, size_t, F*, RootTab,       \
+                                                  cudaStream_t);
 
 }  // namespace whir

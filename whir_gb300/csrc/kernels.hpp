@@ -30,6 +30,16 @@ struct RootTab {
   int log_order;
 };
 
+// Where a kernel publishes a small result for a host that polls host-mapped memory: `data` receives
+// the bytes, flag[1] the context's device error word (*dev_err), then flag[0] = seq after a
+// system-wide fence.
+struct MailSlot {
+  uint8_t* data = nullptr;
+  unsigned int* flag = nullptr;
+  unsigned int seq = 0;
+  const unsigned int* dev_err = nullptr;
+};
+
 // In-place conversion between the canonical limbs of the C ABI and the in-memory form of F
 // (a no-op for the Goldilocks family; Montgomery form for Field192/Field256).
 template <class F>
@@ -90,6 +100,19 @@ cudaError_t launch_encode(const EncodePlan& plan, const F* src, size_t n_msgs, s
                           uint32_t* leaves, int hash_kind, F* scratch, RootTab rt, cudaStream_t s,
                           const EncodeStaging* staging = nullptr);
 
+// Four-step pass 1 of one message of one coset (plan.mode == 1, codeword length = coset size) from
+// its nonzero coefficients grouped by column: column q is j2 = col_j2[q] with entries
+// [col_off[q], col_off[q + 1]) of (ent_j1, ent_val) (coefficient index j1 * C2 + j2). Writes those
+// columns of the intermediate `inter` (plan.scratch_elems elements), whose other entries the caller
+// zeroes; launch_encode_rows_pass then finishes the transform.
+template <class F>
+cudaError_t launch_sparse_cols(const EncodePlan& plan, const uint32_t* col_j2, const uint32_t* col_off,
+                               const uint32_t* ent_j1, const F* ent_val, size_t ncols, F* inter, RootTab rt,
+                               cudaStream_t s);
+template <class F>
+cudaError_t launch_encode_rows_pass(const EncodePlan& plan, const F* scratch, size_t n_msgs, size_t msg_len, F* dst,
+                                    RootTab rt, cudaStream_t s);
+
 // Several independent interleaved encodes (jobs of possibly different shapes, one field) in one
 // launch per pass: the CTAs of a launch are split among the jobs by a device table of per-job
 // arguments (encode_multi_prepare fills its host image; upload it, then launch_encode_multi).
@@ -135,7 +158,9 @@ cudaError_t launch_merkle_multi(const std::vector<MerkleMultiLaunch>& launches, 
 // [leaves (2^layers)][layer 1]...[root] (merkle_tree.rs:96-121). Each launch hashes tiles of
 // 2^tile_log nodes up tile_log layers (tile_log <= 0: the tuned height for this tree, or
 // merkle_tile_log, 10, when none is recorded).
-cudaError_t launch_merkle(uint32_t* nodes, int layers, int hash_kind, cudaStream_t s, int tile_log = 0);
+// When mail.data is set (layers >= 1), the launch that computes the root also publishes it (32 bytes).
+cudaError_t launch_merkle(uint32_t* nodes, int layers, int hash_kind, cudaStream_t s, int tile_log = 0,
+                          const MailSlot& mail = MailSlot());
 extern int merkle_tile_log;
 
 // count messages of `size` bytes (size % 4 == 0) -> count digests.
@@ -143,9 +168,10 @@ cudaError_t launch_hash_many(const uint8_t* in, size_t size, size_t count, uint8
                              cudaStream_t s);
 
 // Searches nonces [start, start + count) and atomically lowers *best to any nonce whose digest's
-// first 8 bytes (LE) are <= threshold (proof_of_work.rs:68-166).
+// first 8 bytes (LE) are <= threshold (proof_of_work.rs:68-166). best[1] must be zero: it counts
+// finished CTAs, and when mail.data is set the last one publishes best[0] (8 bytes) there.
 cudaError_t launch_pow(const uint32_t challenge[8], uint64_t threshold, uint64_t start, uint64_t count,
-                       unsigned long long* best, int hash_kind, cudaStream_t s);
+                       unsigned long long* best, int hash_kind, cudaStream_t s, const MailSlot& mail = MailSlot());
 
 // out[i*cols .. (i+1)*cols) = matrix[idx[i]*cols ..]
 template <class F>

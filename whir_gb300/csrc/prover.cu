@@ -302,7 +302,23 @@ MailFetch mail_begin(whir_ctx* ctx, void* dst0, const void* src0, size_t b0, voi
   }
   return f;
 }
-// Waits (bounded) for a fetch started by mail_begin and copies its bytes out of the mail area.
+// A fetch whose bytes a kernel publishes itself (into the mail area, then the returned slot's
+// sequence number): pass the slot to that kernel's launch, then wait with mail_end.
+MailFetch mail_expect(whir_ctx* ctx, void* dst, size_t bytes, MailSlot* slot) {
+  MailFetch f;
+  f.dst0 = dst;
+  f.b0 = bytes;
+  f.seq = ++ctx->mail_seq;
+  f.done = false;
+  ctx->d2h_bytes += bytes;
+  slot->data = ctx->mail_d + MAIL_DATA_OFF;
+  slot->flag = reinterpret_cast<unsigned int*>(ctx->mail_d + MAIL_FLAG_OFF);
+  slot->seq = f.seq;
+  slot->dev_err = ctx->sc_counter + 3;
+  return f;
+}
+// Waits (bounded) for a fetch started by mail_begin or mail_expect and copies its bytes out of the
+// mail area.
 void mail_end(whir_ctx* ctx, MailFetch& f) {
   if (f.done) return;
   const unsigned int* flag_h = reinterpret_cast<const unsigned int*>(ctx->mail_h + MAIL_FLAG_OFF);
@@ -479,14 +495,17 @@ uint64_t grind(whir_ctx* ctx, int kind, const uint8_t chal[32], uint64_t thresho
   while ((double)chunk < 64.0 * expect && chunk < (1ull << 36)) chunk <<= 1;
   const uint64_t limit = 1ull << 50;
   for (uint64_t start = 0; start < limit; start += chunk) {
-    const unsigned long long init[2] = {~0ull, 0ull};  // best nonce, claimed-block counter
+    const unsigned long long init[2] = {~0ull, 0ull};  // best nonce, finished-CTA counter
     h2d(ctx, ctx->d_pow, init, sizeof(init));
+    unsigned long long best;
+    MailSlot slot;
+    MailFetch f = mail_expect(ctx, &best, sizeof(best), &slot);
     {
       ProfScope prof(ctx, PF_POW);
-      CU(launch_pow(cw, threshold, start, chunk, ctx->d_pow, kind, ctx->stream));
+      CU(launch_pow(cw, threshold, start, chunk, ctx->d_pow, kind, ctx->stream, slot));
     }
-    unsigned long long best;
-    d2h(ctx, &best, ctx->d_pow, sizeof(best));
+    mail_end(ctx, f);
+    ctx->up_off = 0;  // nothing was enqueued after the search, so every earlier upload has completed
     if (best != ~0ull) return best;
   }
   throw Error(WHIR_ERR_POW, "Proof of Work failed to solve.");
@@ -582,11 +601,19 @@ void encode_and_tree(whir_ctx* ctx, const F* d_msgs, size_t n_msgs, size_t msg_l
   fence.armed = false;  // the encode enqueued the waits
   // A wait captures the event's state when it is enqueued, so the events can be reused at once.
   for (cudaEvent_t e : ready) ctx->event_pool.push_back(e);
-  {
-    ProfScope prof(ctx, PF_MERKLE);
-    CU(launch_merkle(w.nodes.p, (int)w.layers, kind, ctx->stream));
+  if (w.layers >= 1) {
+    // the Merkle launch that computes the root publishes it to the host
+    MailSlot slot;
+    MailFetch f = mail_expect(ctx, w.root, 32, &slot);
+    {
+      ProfScope prof(ctx, PF_MERKLE);
+      CU(launch_merkle(w.nodes.p, (int)w.layers, kind, ctx->stream, 0, slot));
+    }
+    mail_end(ctx, f);
+    ctx->up_off = 0;  // nothing was enqueued after the tree, so every earlier upload has completed
+  } else {
+    d2h(ctx, w.root, w.nodes.p, 32);
   }
-  d2h(ctx, w.root, w.nodes.p + ((2ull << w.layers) - 2) * 8, 32);
 }
 
 template <class T, class S>
@@ -1174,19 +1201,50 @@ void accumulate_in_domain(whir_ctx* ctx, T* cov, size_t len, const std::vector<T
       vals.push_back(p.second);
     }
   }
-  DBuf<T> dense(ctx, N), out(ctx, N);
-  DBuf<uint64_t> di(ctx, idx.size());
-  DBuf<T> dv(ctx, vals.size());
-  CU(cudaMemsetAsync(dense.p, 0, N * sizeof(T), ctx->stream));
-  h2d(ctx, di.p, idx.data(), idx.size() * sizeof(uint64_t));
-  h2d(ctx, dv.p, vals.data(), vals.size() * sizeof(T));
-  CU(launch_scatter<T>(dense.p, di.p, dv.p, idx.size(), ctx->stream));
   EncodePlan plan;
   int rc = plan_encode(1, N, N, sizeof(T), &plan);
   if (rc) throw Error(rc, "NTT shape unsupported on the device");
-  DBuf<T> scratch(ctx, plan.scratch_elems);
-  CU(launch_encode<T>(plan, dense.p, 1, N, out.p, nullptr, HASH_BLAKE3, scratch.p, root_tab<typename T::Base>(ctx),
-                      ctx->stream));
+  DBuf<T> out(ctx, N), scratch(ctx, plan.scratch_elems);
+  if (plan.mode == 1) {
+    // Four-step: with a few hundred nonzeros among N coefficients nearly every column of the
+    // (C1 x C2) view is zero, so pass 1 is computed only for the nonzero columns, straight from the
+    // sparse list (the intermediate is zeroed first), and pass 2 runs as usual.
+    const uint64_t C2 = 1ull << plan.logC2;
+    std::vector<std::pair<uint64_t, size_t>> bycol;  // (column j2, entry)
+    for (size_t e = 0; e < idx.size(); ++e) bycol.push_back({idx[e] & (C2 - 1), e});
+    std::sort(bycol.begin(), bycol.end());
+    std::vector<uint32_t> col_j2, col_off, ent_j1;
+    std::vector<T> ent_val;
+    for (const auto& ce : bycol) {
+      if (col_j2.empty() || col_j2.back() != ce.first) {
+        col_j2.push_back((uint32_t)ce.first);
+        col_off.push_back((uint32_t)ent_j1.size());
+      }
+      ent_j1.push_back((uint32_t)(idx[ce.second] >> plan.logC2));
+      ent_val.push_back(vals[ce.second]);
+    }
+    col_off.push_back((uint32_t)ent_j1.size());
+    DBuf<uint32_t> dj2(ctx, col_j2.size()), doff(ctx, col_off.size()), dj1(ctx, ent_j1.size());
+    DBuf<T> dval(ctx, ent_val.size());
+    h2d(ctx, dj2.p, col_j2.data(), col_j2.size() * sizeof(uint32_t));
+    h2d(ctx, doff.p, col_off.data(), col_off.size() * sizeof(uint32_t));
+    h2d(ctx, dj1.p, ent_j1.data(), ent_j1.size() * sizeof(uint32_t));
+    h2d(ctx, dval.p, ent_val.data(), ent_val.size() * sizeof(T));
+    CU(cudaMemsetAsync(scratch.p, 0, plan.scratch_elems * sizeof(T), ctx->stream));
+    CU(launch_sparse_cols<T>(plan, dj2.p, doff.p, dj1.p, dval.p, col_j2.size(), scratch.p,
+                             root_tab<typename T::Base>(ctx), ctx->stream));
+    CU(launch_encode_rows_pass<T>(plan, scratch.p, 1, N, out.p, root_tab<typename T::Base>(ctx), ctx->stream));
+  } else {
+    DBuf<T> dense(ctx, N);
+    DBuf<uint64_t> di(ctx, idx.size());
+    DBuf<T> dv(ctx, vals.size());
+    CU(cudaMemsetAsync(dense.p, 0, N * sizeof(T), ctx->stream));
+    h2d(ctx, di.p, idx.data(), idx.size() * sizeof(uint64_t));
+    h2d(ctx, dv.p, vals.data(), vals.size() * sizeof(T));
+    CU(launch_scatter<T>(dense.p, di.p, dv.p, idx.size(), ctx->stream));
+    CU(launch_encode<T>(plan, dense.p, 1, N, out.p, nullptr, HASH_BLAKE3, scratch.p,
+                        root_tab<typename T::Base>(ctx), ctx->stream));
+  }
   CU(launch_add<T>(cov, out.p, len, ctx->stream));
 }
 
