@@ -26,7 +26,7 @@ namespace whir {
 
 static constexpr int ENC_THREADS = 256;
 static constexpr size_t ENC_SMEM_BUDGET = 64 * 1024;  // data bytes per CTA
-static constexpr int ENC_MAX_LOGN_SMEM = 12;          // largest in-CTA NTT
+static constexpr int ENC_MAX_LOGN_SMEM = ENC_MAX_NTT_LOG;  // largest in-CTA NTT
 // Dynamic shared memory limit set on the encode kernels: the data tile plus at most as many bytes
 // of twiddles (n - 1 base elements for a size-n NTT) plus alignment slack.
 static constexpr size_t ENC_SMEM_ATTR = 2 * ENC_SMEM_BUDGET + 256;
@@ -222,6 +222,7 @@ struct EncArgs {
   uint64_t m_magic;  // ceil(2^32 / M): i / M = (i * m_magic) >> 32 exactly for i * M < 2^32
   int logC, logN, logC1, logC2;
   int mode;    // rows kernel: 0 single pass, 1 four-step pass 2
+  uint64_t add_rows;  // rows kernel without leaves: 0 stores the codeword; else adds rows < add_rows into dst
   int G;       // cosets per CTA (rows mode 0)
   int W;       // columns per CTA (cols kernel)
   RootTab rt;
@@ -316,12 +317,21 @@ __device__ __forceinline__ void encode_rows_body(const EncArgs<F>& a, uint64_t b
     const int logM = __ffs(M) - 1, m = threadIdx.x & (M - 1), rho0 = threadIdx.x >> logM;
     const int rs = ENC_THREADS >> logM, iters = (R * M + ENC_THREADS - 1) / ENC_THREADS;
     const int sb = swz<F>((m << logn) + brev(rho0, logn));
-    F* q = a.dst + (c_base * C + k1 + ((uint64_t)rho0 << a.logC1)) * M + m;
-    const uint64_t qstep = ((uint64_t)rs << a.logC1) * M;
-    #pragma unroll 4
-    for (int i = 0; i < iters; ++i) {
-      if (threadIdx.x + i * ENC_THREADS < R * M) *q = lds(s, sb ^ swz<F>(brev(i * rs, logn)));
-      q += qstep;
+    const uint64_t row0 = c_base * C + k1 + ((uint64_t)rho0 << a.logC1), rstep = (uint64_t)rs << a.logC1;
+    F* q = a.dst + row0 * M + m;
+    const uint64_t qstep = rstep * M;
+    if (a.add_rows) {
+      for (int i = 0; i < iters; ++i) {
+        if (threadIdx.x + i * ENC_THREADS < R * M && row0 + i * rstep < a.add_rows)
+          *q = *q + lds(s, sb ^ swz<F>(brev(i * rs, logn)));
+        q += qstep;
+      }
+    } else {
+      #pragma unroll 4
+      for (int i = 0; i < iters; ++i) {
+        if (threadIdx.x + i * ENC_THREADS < R * M) *q = lds(s, sb ^ swz<F>(brev(i * rs, logn)));
+        q += qstep;
+      }
     }
   } else {
     #pragma unroll 4
@@ -337,7 +347,10 @@ __device__ __forceinline__ void encode_rows_body(const EncArgs<F>& a, uint64_t b
         row = c_base * C + k1 + ((uint64_t)rho << a.logC1);
         sidx = (m << logn) + brev(rho, logn);
       }
-      a.dst[row * M + m] = lds(s, swz<F>(sidx));
+      if (a.add_rows == 0)
+        a.dst[row * M + m] = lds(s, swz<F>(sidx));
+      else if (row < a.add_rows)
+        a.dst[row * M + m] = a.dst[row * M + m] + lds(s, swz<F>(sidx));
     }
   }
   if (a.leaves == nullptr) return;
@@ -607,6 +620,7 @@ cudaError_t launch_encode(const EncodePlan& p, const F* src, size_t n_msgs, size
     return staging ? cudaStreamWaitEvent(s, staging->ready[g], 0) : cudaSuccess;
   };
   EncArgs<F> a;
+  a.add_rows = 0;
   a.leaves = leaves;
   a.msg_len = msg_len;
   a.M = (int)n_msgs;
@@ -692,12 +706,15 @@ cudaError_t launch_sparse_cols(const EncodePlan& p, const uint32_t* col_j2, cons
 }
 
 // Pass 2 alone (the four-step row pass) of an encode whose intermediate `scratch` was produced
-// elsewhere (launch_sparse_cols); no leaf hashing.
+// elsewhere (launch_sparse_cols); no leaf hashing. With add_rows > 0 (one message) the evaluations
+// at rows < add_rows are added into dst instead of being stored.
 template <class F>
 cudaError_t launch_encode_rows_pass(const EncodePlan& p, const F* scratch, size_t n_msgs, size_t msg_len, F* dst,
-                                    RootTab rt, cudaStream_t s) {
+                                    RootTab rt, cudaStream_t s, size_t add_rows) {
   if (p.mode != 1 || p.logN > rt.log_order || p.logN > 32) return cudaErrorInvalidValue;
+  if (add_rows && n_msgs != 1) return cudaErrorInvalidValue;
   EncArgs<F> a;
+  a.add_rows = add_rows;
   a.leaves = nullptr;
   a.msg_len = msg_len;
   a.M = (int)n_msgs;
@@ -728,6 +745,7 @@ size_t encode_multi_table_bytes(size_t njobs) {
 template <class F>
 static EncArgs<F> enc_args_of(const EncodeJobDesc& d, RootTab rt) {
   EncArgs<F> a;
+  a.add_rows = 0;
   a.leaves = d.leaves;
   a.msg_len = d.msg_len;
   a.M = (int)d.n_msgs;
@@ -898,6 +916,6 @@ cudaError_t launch_to_canonical(F* v, size_t n, cudaStream_t s) {
   template cudaError_t launch_sparse_cols<F>(const EncodePlan&, const uint32_t*, const uint32_t*, const uint32_t*,  \
                                              const F*, size_t, F*, RootTab, cudaStream_t);                        \
   template cudaError_t launch_encode_rows_pass<F>(const EncodePlan&, const F*, size_t, size_t, F*, RootTab,       \
-                                                  cudaStream_t);
+                                                  cudaStream_t, size_t);
 
 }  // namespace whir

@@ -67,6 +67,9 @@ int plan_encode_default(size_t n_msgs, size_t msg_len, size_t codeword_len, size
 struct EncodeTuning {
   int mode, logC2, W, G;
 };
+// Largest NTT an encode CTA runs in shared memory (log2 points): a four-step pass transforms at most
+// 2^ENC_MAX_NTT_LOG points.
+static constexpr int ENC_MAX_NTT_LOG = 12;
 int plan_encode_tuned(size_t n_msgs, size_t msg_len, size_t codeword_len, size_t elem_bytes, const EncodeTuning& t,
                       EncodePlan* plan);
 // Process-wide table of tuned choices (encode plans by shape, Merkle tile heights by tree height),
@@ -111,7 +114,7 @@ cudaError_t launch_sparse_cols(const EncodePlan& plan, const uint32_t* col_j2, c
                                cudaStream_t s);
 template <class F>
 cudaError_t launch_encode_rows_pass(const EncodePlan& plan, const F* scratch, size_t n_msgs, size_t msg_len, F* dst,
-                                    RootTab rt, cudaStream_t s);
+                                    RootTab rt, cudaStream_t s, size_t add_rows = 0);
 
 // Several independent interleaved encodes (jobs of possibly different shapes, one field) in one
 // launch per pass: the CTAs of a launch are split among the jobs by a device table of per-job

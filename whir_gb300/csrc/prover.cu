@@ -1202,9 +1202,15 @@ void accumulate_in_domain(whir_ctx* ctx, T* cov, size_t len, const std::vector<T
     }
   }
   EncodePlan plan;
-  int rc = plan_encode(1, N, N, sizeof(T), &plan);
+  // Four-step with 2^10-point row transforms where the size allows (2^21: 2048 CTAs of 2^10 points
+  // fill the GPU in several waves; the largest tile, 512 CTAs of 2^12 points, left most of a second
+  // wave idle), and the plain plan otherwise.
+  const int logN_ = (int)layers_for(N);
+  const EncodeTuning four{1, std::max(logN_ - ENC_MAX_NTT_LOG, std::min(10, logN_ - 1)), 1, 1};
+  int rc = logN_ > ENC_MAX_NTT_LOG ? plan_encode_tuned(1, N, N, sizeof(T), four, &plan) : -1;
+  if (rc) rc = plan_encode(1, N, N, sizeof(T), &plan);
   if (rc) throw Error(rc, "NTT shape unsupported on the device");
-  DBuf<T> out(ctx, N), scratch(ctx, plan.scratch_elems);
+  DBuf<T> scratch(ctx, plan.scratch_elems);
   if (plan.mode == 1) {
     // Four-step: with a few hundred nonzeros among N coefficients nearly every column of the
     // (C1 x C2) view is zero, so pass 1 is computed only for the nonzero columns, straight from the
@@ -1233,9 +1239,10 @@ void accumulate_in_domain(whir_ctx* ctx, T* cov, size_t len, const std::vector<T
     CU(cudaMemsetAsync(scratch.p, 0, plan.scratch_elems * sizeof(T), ctx->stream));
     CU(launch_sparse_cols<T>(plan, dj2.p, doff.p, dj1.p, dval.p, col_j2.size(), scratch.p,
                              root_tab<typename T::Base>(ctx), ctx->stream));
-    CU(launch_encode_rows_pass<T>(plan, scratch.p, 1, N, out.p, root_tab<typename T::Base>(ctx), ctx->stream));
+    // pass 2 adds the evaluations at the first len points straight into the covector
+    CU(launch_encode_rows_pass<T>(plan, scratch.p, 1, N, cov, root_tab<typename T::Base>(ctx), ctx->stream, len));
   } else {
-    DBuf<T> dense(ctx, N);
+    DBuf<T> dense(ctx, N), out(ctx, N);
     DBuf<uint64_t> di(ctx, idx.size());
     DBuf<T> dv(ctx, vals.size());
     CU(cudaMemsetAsync(dense.p, 0, N * sizeof(T), ctx->stream));
@@ -1244,8 +1251,8 @@ void accumulate_in_domain(whir_ctx* ctx, T* cov, size_t len, const std::vector<T
     CU(launch_scatter<T>(dense.p, di.p, dv.p, idx.size(), ctx->stream));
     CU(launch_encode<T>(plan, dense.p, 1, N, out.p, nullptr, HASH_BLAKE3, scratch.p,
                         root_tab<typename T::Base>(ctx), ctx->stream));
+    CU(launch_add<T>(cov, out.p, len, ctx->stream));
   }
-  CU(launch_add<T>(cov, out.p, len, ctx->stream));
 }
 
 template <class T>
