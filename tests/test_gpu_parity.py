@@ -133,7 +133,7 @@ def test_merkle_parity(ctx, orc, engine, n):
 
 
 @pytest.mark.parametrize("fname,fid", FIELDS)
-@pytest.mark.parametrize("n", [1, 2, 4, 8, 1 << 10, 1 << 16, 1 << 18])
+@pytest.mark.parametrize("n", [1, 2, 4, 8, 1 << 10, 1 << 16, 1 << 18, 1 << 20])
 def test_sumcheck_fold_parity(ctx, orc, fname, fid, n):
     rng = Rng(n + fid)
     L = W.TARGET_LIMBS[fid]

@@ -202,6 +202,144 @@ __global__ void __launch_bounds__(SC_THREADS) sc_fold_compute_kernel(T* a, T* b,
   finish_pairs(acc0, acc2, partials, out, counter);
 }
 
+// Raises a kernel's dynamic shared-memory limit to `bytes` once per device (the flags and results
+// belong to the caller's instantiation).
+static constexpr int SC_MAX_DEVICES = 64;
+template <class K>
+static cudaError_t sc_smem_attr_once(K kernel, size_t bytes, std::once_flag* flags, cudaError_t* results) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= SC_MAX_DEVICES)
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  std::call_once(flags[dev], [&] {
+    results[dev] = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  });
+  return results[dev];
+}
+
+// Large rounds (n >= SC_BULK_MIN) with the operands staged by the bulk-copy engine. A tile is
+// SC_THREADS consecutive items i (pairs (i, i + h) of a round without fold, quads
+// (i, i + q, i + h, i + h + q) of a fold-and-compute round); its segments of a and b (4 KiB each for
+// 16-byte elements) go through two shared-memory stages filled by cp.async.bulk against per-stage
+// mbarriers, so the next tile's loads are in flight while this tile is folded and accumulated, with
+// no registers held for them. CTAs take tiles t = blockIdx.x + k gridDim.x. Waits are bounded as in
+// the tensor sums; a timeout sets the context's sticky device error word (counter[3]), which the
+// next host-mapped publication reports, and the CTA stops reading.
+static constexpr uint64_t SC_BULK_MIN = 1ull << 18;
+static constexpr int SC_BULK_NST = 2;
+
+template <class T, bool FOLD>
+__global__ void __launch_bounds__(SC_THREADS, 2) sc_round_bulk_kernel(T* a, T* b, uint64_t n, T r, T* partials,
+                                                                      T* out, unsigned int* counter) {
+  constexpr int NSEG = FOLD ? 8 : 4;
+  constexpr uint32_t SEG = SC_THREADS * sizeof(T), STAGE = NSEG * SEG;
+  extern __shared__ __align__(128) unsigned char rb_smem[];
+  __shared__ __align__(8) uint64_t bar[SC_BULK_NST];
+  __shared__ int aborted;
+  const uint64_t h = n >> 1, q = n >> 2, items = FOLD ? q : h;
+  const uint64_t tiles = items / SC_THREADS;
+  const int ntile = (int)((tiles - blockIdx.x + gridDim.x - 1) / gridDim.x);  // tiles of this CTA
+  if (threadIdx.x == 0) {
+    aborted = 0;
+    for (int st = 0; st < SC_BULK_NST; ++st) mbar_init(&bar[st], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  // segment k of tile t starts at element off[k] + t * SC_THREADS of a (k < NSEG / 2) or b
+  auto issue = [&](int k) {
+    const int st = k % SC_BULK_NST;
+    const uint64_t i0 = (blockIdx.x + (uint64_t)k * gridDim.x) * SC_THREADS;
+    unsigned char* dst = rb_smem + (size_t)st * STAGE;
+    mbar_arrive_expect_tx(&bar[st], STAGE);
+#pragma unroll
+    for (int sg = 0; sg < NSEG; ++sg) {
+      const T* base = sg < NSEG / 2 ? a : b;
+      const int part = sg % (NSEG / 2);
+      const uint64_t off = FOLD ? ((part & 1) ? q : 0) + ((part & 2) ? h : 0) : (part ? h : 0);
+      bulk_copy_g2s(dst + sg * SEG, base + off + i0, SEG, &bar[st]);
+    }
+  };
+  if (threadIdx.x == 0)
+    for (int k = 0; k < ntile && k < SC_BULK_NST; ++k) issue(k);
+  WideAcc<T> w0, w2;
+  w0.init();
+  w2.init();
+  int k = 0;
+  for (; k < ntile; ++k) {
+    const int st = k % SC_BULK_NST;
+    if (mbar_wait(&bar[st], (uint32_t)(k / SC_BULK_NST) & 1)) {
+      const T* v = reinterpret_cast<const T*>(rb_smem + (size_t)st * STAGE) + threadIdx.x;
+      const uint64_t i = (blockIdx.x + (uint64_t)k * gridDim.x) * SC_THREADS + threadIdx.x;
+      if constexpr (FOLD) {
+        const T a0 = v[0], a1 = v[SC_THREADS], a2 = v[2 * SC_THREADS], a3 = v[3 * SC_THREADS];
+        const T b0 = v[4 * SC_THREADS], b1 = v[5 * SC_THREADS], b2 = v[6 * SC_THREADS], b3 = v[7 * SC_THREADS];
+        const T fa0 = a0 + (a2 - a0) * r, fa1 = a1 + (a3 - a1) * r;
+        const T fb0 = b0 + (b2 - b0) * r, fb1 = b1 + (b3 - b1) * r;
+        a[i] = fa0;
+        a[i + q] = fa1;
+        b[i] = fb0;
+        b[i + q] = fb1;
+        w0.mac(fa0, fb0);
+        w2.mac(fa1 - fa0, fb1 - fb0);
+      } else {
+        const T a0 = v[0], a1 = v[SC_THREADS], b0 = v[2 * SC_THREADS], b1 = v[3 * SC_THREADS];
+        w0.mac(a0, b0);
+        w2.mac(a1 - a0, b1 - b0);
+      }
+    } else {
+      aborted = 1;
+    }
+    __syncthreads();
+    if (aborted) break;
+    if (threadIdx.x == 0 && k + SC_BULK_NST < ntile) {
+      fence_proxy_async_smem();
+      issue(k + SC_BULK_NST);
+    }
+  }
+  if (aborted && threadIdx.x == 0) {
+    atomicExch(counter + 3, 1u);
+    for (int j = k; j < ntile && j < k + SC_BULK_NST; ++j) mbar_wait(&bar[j % SC_BULK_NST], (uint32_t)(j / SC_BULK_NST) & 1);
+  }
+  T acc0 = w0.get(), acc2 = w2.get();
+  finish_pairs(acc0, acc2, partials, out, counter);
+}
+
+template <class T, bool FOLD>
+static cudaError_t run_round_bulk(T* a, T* b, size_t n, T r, T* partials, size_t* nparts, cudaStream_t s, T* out,
+                                  unsigned int* counter) {
+  static std::once_flag flags[SC_MAX_DEVICES];
+  static cudaError_t results[SC_MAX_DEVICES];
+  constexpr size_t smem = (size_t)SC_BULK_NST * (FOLD ? 8 : 4) * SC_THREADS * sizeof(T);
+  cudaError_t e = sc_smem_attr_once(sc_round_bulk_kernel<T, FOLD>, smem, flags, results);
+  if (e != cudaSuccess) return e;
+  // Two resident CTAs per SM; tiles split evenly (a CTA with one tile more than the others would set
+  // the time). The partials area holds SC_MAX_BLOCKS pairs.
+  static const size_t slots = [] {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+        cudaSuccess || sms < 1)
+      sms = 152;
+    return (size_t)std::min<size_t>(2 * (size_t)sms, SC_MAX_BLOCKS);
+  }();
+  const uint64_t tiles = (FOLD ? n / 4 : n / 2) / SC_THREADS;
+  const uint64_t per = (tiles + slots - 1) / slots;
+  const size_t g = (size_t)std::max<uint64_t>(1, (tiles + per - 1) / per);
+  sc_round_bulk_kernel<T, FOLD><<<(unsigned)g, SC_THREADS, smem, s>>>(a, b, n, r, partials, out, counter);
+  note_launch();
+  *nparts = g;
+  return cudaGetLastError();
+}
+
+// The bulk-staged round takes power-of-two n >= SC_BULK_MIN and 16-byte aligned vectors.
+template <class T>
+static bool round_bulk_ok(const T* a, const T* b, size_t n) {
+  // (segments of SC_THREADS elements and offsets that are multiples of SC_THREADS elements keep every
+  // copy 16-byte aligned for 8-, 16-, 24- and 32-byte elements)
+  return n >= SC_BULK_MIN && (n & (n - 1)) == 0 && sizeof(T) % 8 == 0 && sizeof(T) <= 32 &&
+         reinterpret_cast<uintptr_t>(a) % 16 == 0 && reinterpret_cast<uintptr_t>(b) % 16 == 0;
+}
+
 // Rounds on vectors of at most SC_SMALL elements run in one warp: no shared memory, no barriers, no
 // cross-block partials and little code to fetch. These launches are latency-bound: event-timed on a
 // GB300, a fold-and-compute round at n = 16 takes 8.1 us this way against 12.6 us with the
@@ -324,6 +462,9 @@ cudaError_t launch_sumcheck_compute(const T* a, const T* b, size_t n, T* partial
     *nparts = 1;
     return cudaGetLastError();
   }
+  if (round_bulk_ok(a, b, n))
+    return run_round_bulk<T, false>(const_cast<T*>(a), const_cast<T*>(b), n, T::zero(), partials, nparts, s, out,
+                                    counter);
   size_t g = sumcheck_partials(n);
   sc_compute_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(a, b, n, partials, out, counter);
   note_launch();
@@ -339,6 +480,7 @@ cudaError_t launch_fold_compute(T* a, T* b, size_t n, T r, T* partials, size_t* 
     *nparts = 1;
     return cudaGetLastError();
   }
+  if (round_bulk_ok(a, b, n)) return run_round_bulk<T, true>(a, b, n, r, partials, nparts, s, out, counter);
   size_t g = sumcheck_partials(n);
   sc_fold_compute_kernel<T><<<(unsigned)g, SC_THREADS, 0, s>>>(a, b, n, r, partials, out, counter);
   note_launch();
@@ -1370,22 +1512,6 @@ __global__ void tensor_table_kernel(const T* ab, int cnt, T scalar, T* out) {
     for (int q = 0; q < cnt; ++q) v = v * ab[2 * q + ((e >> (cnt - 1 - q)) & 1)];
     out[e] = v;
   }
-}
-
-// Raises a kernel's dynamic shared-memory limit to `bytes` once per device (the flags and results
-// belong to the caller's instantiation).
-static constexpr int SC_MAX_DEVICES = 64;
-template <class K>
-static cudaError_t sc_smem_attr_once(K kernel, size_t bytes, std::once_flag* flags, cudaError_t* results) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= SC_MAX_DEVICES)
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  std::call_once(flags[dev], [&] {
-    results[dev] = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  });
-  return results[dev];
 }
 
 template <class T, class S, int NF>
