@@ -339,13 +339,18 @@ inline TensorShape tensor_plan(int nvars, int k, int nvec, int nforms, uint64_t 
 
 template <class T, class S>
 cudaError_t launch_tensor_sums(const S* x, const TensorShape& sh, const T* tables, T* partials, T* out,
-                               unsigned int* counter, cudaStream_t s);
+                               unsigned int* counter, cudaStream_t s,
+                               const MailSlot& mail = MailSlot());
 template <class T, class S>
 cudaError_t launch_tensor_fold(const S* x, const TensorShape& sh, const T* w, const T* kf, const T* tables, T* a_out,
                                T* b_out, unsigned int* err, cudaStream_t s);
 // out[e] = scalar * prod_q (bit_{cnt-1-q}(e) ? ab[2q+1] : ab[2q]) for e < 2^cnt (device arrays).
 template <class T>
 cudaError_t launch_tensor_table(const T* ab, int cnt, T scalar, T* out, cudaStream_t s);
+// Every form's row table (2^R) and column table (2^C) in one launch, from 2 (R + C) (alpha, beta)
+// values per form; out holds nforms x (2^R + 2^C) entries, form-major, rows first.
+template <class T>
+cudaError_t launch_tensor_tables(const T* ab, int nforms, int R, int C, T* out, cudaStream_t s);
 
 // dst[i] = map(v0[i]) + sum_{j>=1} coeffs[j] * v_j[i]  (lift + mixed_scalar_mul_add, algebra/mod.rs:51-98)
 template <class T, class S>

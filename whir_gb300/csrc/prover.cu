@@ -1097,13 +1097,18 @@ std::vector<T> initial_sumcheck_tensor(whir_ctx* ctx, const Sumcheck& c, Transcr
       }
     DBuf<T> dab(ctx, std::max<size_t>(ab.size(), 1));
     h2d(ctx, dab.p, ab.data(), ab.size() * sizeof(T));
-    const size_t pf = 2 * (size_t)(nvars - k);
-    for (int f = 0; f < NF; ++f) {
-      CU(launch_tensor_table<T>(dab.p + f * pf, sh.R, T::one(), tables.p + f * per, ctx->stream));
-      CU(launch_tensor_table<T>(dab.p + f * pf + 2 * sh.R, sh.C, T::one(), tables.p + f * per + rows, ctx->stream));
+    CU(launch_tensor_tables<T>(dab.p, NF, sh.R, sh.C, tables.p, ctx->stream));
+    if (V.size() * sizeof(T) <= MAIL_DATA_BYTES) {
+      // the last CTA of the sums pass publishes the sums to the host itself
+      MailSlot slot;
+      MailFetch fetch = mail_expect(ctx, V.data(), V.size() * sizeof(T), &slot);
+      CU((launch_tensor_sums<T, S>(x, sh, tables.p, parts.p, out.p, ctx->sc_counter, ctx->stream, slot)));
+      mail_end(ctx, fetch);
+      ctx->up_off = 0;  // nothing was enqueued after the sums, so every earlier upload has completed
+    } else {
+      CU((launch_tensor_sums<T, S>(x, sh, tables.p, parts.p, out.p, ctx->sc_counter, ctx->stream)));
+      d2h(ctx, V.data(), out.p, V.size() * sizeof(T));
     }
-    CU((launch_tensor_sums<T, S>(x, sh, tables.p, parts.p, out.p, ctx->sc_counter, ctx->stream)));
-    d2h(ctx, V.data(), out.p, V.size() * sizeof(T));
     if (!(V.back() == T::zero())) throw Error(WHIR_ERR_CUDA, "tensor sums: a bulk-copy stage wait timed out");
     V.pop_back();
   }

@@ -1149,7 +1149,7 @@ __device__ __forceinline__ void load_cols(const S* p, S* out) {
 // recorded an error in counter[2] (else 0) and re-arms counter[0] and counter[2].
 template <class T, int NF>
 __device__ __forceinline__ void tensor_sums_finish(const T (&mine)[NF], const TensorShape& sh, T* partials, T* out,
-                                                   unsigned int* counter) {
+                                                   unsigned int* counter, const MailSlot& mail) {
   __shared__ bool am_last;
 #pragma unroll
   for (int f = 0; f < NF; ++f) {
@@ -1165,24 +1165,36 @@ __device__ __forceinline__ void tensor_sums_finish(const T (&mine)[NF], const Te
   __threadfence();
   const uint64_t nz = 1ull << sh.k, groups = sh.row_groups * sh.col_tiles;
   const uint64_t nout = (uint64_t)sh.nvec * NF * nz;
+  T* mo = reinterpret_cast<T*>(mail.data);  // host-mapped copy of out, when publishing
   for (uint64_t o = threadIdx.x; o < nout; o += blockDim.x) {
     const uint64_t zz = o % nz, f = (o / nz) % NF, jj = o / (nz * NF);
     const T* p = partials + ((jj * nz + zz) * groups) * NF + f;
     T s = T::zero();
     for (uint64_t q = 0; q < groups; ++q) s += ldcg_t(p + q * NF);
     out[o] = s;
+    if (mo) mo[o] = s;
   }
   if (threadIdx.x == 0) {
     const unsigned int err = atomicExch(counter + 2, 0u);
     out[nout] = err ? T::one() : T::zero();
+    if (mo) mo[nout] = out[nout];
     counter[0] = 0;
+  }
+  if (mo == nullptr) return;
+  __threadfence_system();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    reinterpret_cast<volatile unsigned int*>(mail.flag)[1] = *reinterpret_cast<const volatile unsigned int*>(mail.dev_err);
+    __threadfence_system();
+    *reinterpret_cast<volatile unsigned int*>(mail.flag) = mail.seq;
   }
 }
 
 static constexpr int TS_RB = 4;
 template <class T, class S, int NF, int CPT>
 __global__ void __launch_bounds__(TS_THREADS) tensor_sums_kernel(const S* x, TensorShape sh, const T* tables,
-                                                                 T* partials, T* out, unsigned int* counter) {
+                                                                 T* partials, T* out, unsigned int* counter,
+                                                                 MailSlot mail) {
   __shared__ T srow[NF][TS_MAX_RPC];
   const uint64_t rows = 1ull << sh.R, cols = 1ull << sh.C, per = rows + cols;
   uint64_t bid = blockIdx.x;
@@ -1250,7 +1262,7 @@ __global__ void __launch_bounds__(TS_THREADS) tensor_sums_kernel(const S* x, Ten
       for (int c = 0; c < CPT; ++c) mine[f] += tables[(uint64_t)f * per + rows + col + c] * acc[f][c].get();
     }
   }
-  tensor_sums_finish<T, NF>(mine, sh, partials, out, counter);
+  tensor_sums_finish<T, NF>(mine, sh, partials, out, counter, mail);
 }
 
 // Sums pass with the tile staged by the bulk-copy engine: CTA (j, z, row group, 512-column tile)
@@ -1279,7 +1291,8 @@ struct TbMinCtas {
 
 template <class T, class S, int NF>
 __global__ void __launch_bounds__(TS_THREADS, TbMinCtas<T, NF>::value) tensor_sums_bulk_kernel(const S* x, TensorShape sh, const T* tables,
-                                                                         T* partials, T* out, unsigned int* counter) {
+                                                                         T* partials, T* out, unsigned int* counter,
+                                                                         MailSlot mail) {
   static_assert(sizeof(S) == 8, "two 8-byte source elements per 16-byte shared load");
   extern __shared__ __align__(128) unsigned char tb_smem[];
   __shared__ T srow[NF][TS_MAX_RPC];
@@ -1366,7 +1379,7 @@ __global__ void __launch_bounds__(TS_THREADS, TbMinCtas<T, NF>::value) tensor_su
       mine[f] += tables[(uint64_t)f * per + rows + col + 1] * acc[f][1].get();
     }
   }
-  tensor_sums_finish<T, NF>(mine, sh, partials, out, counter);
+  tensor_sums_finish<T, NF>(mine, sh, partials, out, counter, mail);
 }
 
 // Fold pass: a_out[i] = sum_{j, z} w[j 2^k + z] x_j(z, i) and b_out[i] = sum_f kf[f] row_f[i >> C]
@@ -1516,13 +1529,13 @@ __global__ void tensor_table_kernel(const T* ab, int cnt, T scalar, T* out) {
 
 template <class T, class S, int NF>
 static cudaError_t run_tensor_sums_bulk(const S* x, const TensorShape& sh, const T* tables, T* partials, T* out,
-                                        unsigned int* counter, cudaStream_t s) {
+                                        unsigned int* counter, cudaStream_t s, const MailSlot& mail) {
   static std::once_flag flags[SC_MAX_DEVICES];
   static cudaError_t results[SC_MAX_DEVICES];
   cudaError_t e = sc_smem_attr_once(tensor_sums_bulk_kernel<T, S, NF>, TB_SMEM, flags, results);
   if (e != cudaSuccess) return e;
   tensor_sums_bulk_kernel<T, S, NF><<<(unsigned)sh.grid(), TS_THREADS, TB_SMEM, s>>>(x, sh, tables, partials, out,
-                                                                                     counter);
+                                                                                     counter, mail);
   return cudaSuccess;
 }
 
@@ -1534,7 +1547,7 @@ inline bool tensor_sums_bulk_ok(const TensorShape& sh, size_t src_bytes) {
 
 template <class T, class S>
 cudaError_t launch_tensor_sums(const S* x, const TensorShape& sh, const T* tables, T* partials, T* out,
-                               unsigned int* counter, cudaStream_t s) {
+                               unsigned int* counter, cudaStream_t s, const MailSlot& mail) {
   const unsigned grid = (unsigned)sh.grid();
   const bool two = sh.cpt == 2;
   if (two && (sizeof(S) != 8 || reinterpret_cast<uintptr_t>(x) % 16)) return cudaErrorInvalidValue;
@@ -1542,10 +1555,10 @@ cudaError_t launch_tensor_sums(const S* x, const TensorShape& sh, const T* table
     if (tensor_sums_bulk_ok(sh, sizeof(S))) {
       cudaError_t e = cudaSuccess;
       switch (sh.nforms) {
-        case 1: e = run_tensor_sums_bulk<T, S, 1>(x, sh, tables, partials, out, counter, s); break;
-        case 2: e = run_tensor_sums_bulk<T, S, 2>(x, sh, tables, partials, out, counter, s); break;
-        case 3: e = run_tensor_sums_bulk<T, S, 3>(x, sh, tables, partials, out, counter, s); break;
-        case 4: e = run_tensor_sums_bulk<T, S, 4>(x, sh, tables, partials, out, counter, s); break;
+        case 1: e = run_tensor_sums_bulk<T, S, 1>(x, sh, tables, partials, out, counter, s, mail); break;
+        case 2: e = run_tensor_sums_bulk<T, S, 2>(x, sh, tables, partials, out, counter, s, mail); break;
+        case 3: e = run_tensor_sums_bulk<T, S, 3>(x, sh, tables, partials, out, counter, s, mail); break;
+        case 4: e = run_tensor_sums_bulk<T, S, 4>(x, sh, tables, partials, out, counter, s, mail); break;
         default: return cudaErrorInvalidValue;
       }
       if (e != cudaSuccess) return e;
@@ -1555,9 +1568,9 @@ cudaError_t launch_tensor_sums(const S* x, const TensorShape& sh, const T* table
   }
 #define WHIR_TS_LAUNCH(NF)                                                                                        \
   if (two)                                                                                                        \
-    tensor_sums_kernel<T, S, NF, 2><<<grid, sh.threads, 0, s>>>(x, sh, tables, partials, out, counter);          \
+    tensor_sums_kernel<T, S, NF, 2><<<grid, sh.threads, 0, s>>>(x, sh, tables, partials, out, counter, mail);    \
   else                                                                                                            \
-    tensor_sums_kernel<T, S, NF, 1><<<grid, sh.threads, 0, s>>>(x, sh, tables, partials, out, counter);
+    tensor_sums_kernel<T, S, NF, 1><<<grid, sh.threads, 0, s>>>(x, sh, tables, partials, out, counter, mail);
   switch (sh.nforms) {
     case 1: WHIR_TS_LAUNCH(1) break;
     case 2: WHIR_TS_LAUNCH(2) break;
@@ -1603,6 +1616,33 @@ cudaError_t launch_tensor_fold(const S* x, const TensorShape& sh, const T* w, co
   const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((len + TS_THREADS - 1) / TS_THREADS,
                                                                            SC_MAX_BLOCKS * 4));
   tensor_fold_kernel<T, S><<<grid, TS_THREADS, smem, s>>>(x, sh, w, kf, tables, a_out, b_out);
+  note_launch();
+  return cudaGetLastError();
+}
+
+// Row and column tables of every form in one launch: form f's entries out[f (2^R + 2^C) + e] are its
+// row table (e < 2^R: variables 0..R-1, pairs ab[f pf ..]) then its column table (variables R..R+C-1,
+// pairs ab[f pf + 2R ..]), pf = 2 (R + C).
+template <class T>
+__global__ void tensor_tables_kernel(const T* ab, int nforms, int R, int C, T* out) {
+  const uint64_t rows = 1ull << R, per = rows + (1ull << C), total = per * (uint64_t)nforms;
+  const uint64_t pf = 2ull * (R + C);
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total; t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t f = t / per, e = t - f * per;
+    const bool is_row = e < rows;
+    const int cnt = is_row ? R : C;
+    const uint64_t idx = is_row ? e : e - rows;
+    const T* p = ab + f * pf + (is_row ? 0 : 2ull * R);
+    T v = T::one();
+    for (int q = 0; q < cnt; ++q) v = v * p[2 * q + ((idx >> (cnt - 1 - q)) & 1)];
+    out[t] = v;
+  }
+}
+template <class T>
+cudaError_t launch_tensor_tables(const T* ab, int nforms, int R, int C, T* out, cudaStream_t s) {
+  const uint64_t total = ((1ull << R) + (1ull << C)) * (uint64_t)nforms;
+  if (total == 0) return cudaSuccess;
+  tensor_tables_kernel<T><<<(unsigned)std::min<uint64_t>((total + 255) / 256, 4096), 256, 0, s>>>(ab, nforms, R, C, out);
   note_launch();
   return cudaGetLastError();
 }
@@ -1712,7 +1752,8 @@ cudaError_t launch_univariate_eval(const S* coeffs, size_t n, T x, T* partials, 
   template cudaError_t launch_add<T>(T*, const T*, size_t, cudaStream_t);                                        \
   template cudaError_t launch_eq_table<T>(const T*, int, int, T, T*, cudaStream_t);                              \
   template cudaError_t launch_rows_finish<T>(T*, size_t, T, const T*, int, const T*, int, int, T*, cudaStream_t);  \
-  template cudaError_t launch_tensor_table<T>(const T*, int, T, T*, cudaStream_t);
+  template cudaError_t launch_tensor_table<T>(const T*, int, T, T*, cudaStream_t);                                \
+  template cudaError_t launch_tensor_tables<T>(const T*, int, int, int, T*, cudaStream_t);
 
 // Kernels that read coefficient vectors over S and compute over T.
 #define WHIR_SC_EMBED_INST(T, S)                                                                                 \
@@ -1726,7 +1767,7 @@ cudaError_t launch_univariate_eval(const S* coeffs, size_t n, T x, T* partials, 
   template cudaError_t launch_rows_fold_compute<T, S>(const S*, size_t, T, const T*, size_t, int, const T*, int,  \
                                                       int, T*, T*, T*, size_t*, cudaStream_t, T*, unsigned int*); \
   template cudaError_t launch_tensor_sums<T, S>(const S*, const TensorShape&, const T*, T*, T*, unsigned int*,     \
-                                                cudaStream_t);                                                   \
+                                                cudaStream_t, const MailSlot&);                                                   \
   template cudaError_t launch_tensor_fold<T, S>(const S*, const TensorShape&, const T*, const T*, const T*, T*, T*, \
                                                 unsigned int*, cudaStream_t);
 
