@@ -579,4 +579,21 @@ cudaError_t launch_gather_digests(const uint32_t* nodes, const uint64_t* idx, si
   return cudaGetLastError();
 }
 
+__global__ void gather_paths_kernel(const uint32_t* nodes, const uint64_t* idx, uint64_t q, int layers, uint32_t* out) {
+  const uint64_t total = q * (uint64_t)layers * 8;
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total; t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t w = t & 7, jl = t >> 3, j = jl / (uint64_t)layers, l = jl - j * (uint64_t)layers;
+    const uint64_t off = (2ull << layers) - (2ull << (layers - l));
+    out[t] = nodes[(off + ((idx[j] >> l) ^ 1)) * 8 + w];
+  }
+}
+cudaError_t launch_gather_paths(const uint32_t* nodes, const uint64_t* idx, size_t q, int layers, uint32_t* out,
+                                cudaStream_t s) {
+  if (q == 0 || layers <= 0) return cudaSuccess;
+  const size_t total = q * (size_t)layers * 8;
+  gather_paths_kernel<<<(unsigned)std::min<size_t>((total + 255) / 256, 4096), 256, 0, s>>>(nodes, idx, q, layers, out);
+  note_launch();
+  return cudaGetLastError();
+}
+
 }  // namespace whir

@@ -181,6 +181,12 @@ template <class F>
 cudaError_t launch_gather_rows(const F* matrix, size_t cols, const uint64_t* idx, size_t n, F* out, cudaStream_t s);
 cudaError_t launch_gather_digests(const uint32_t* nodes, const uint64_t* idx, size_t n, uint32_t* out,
                                   cudaStream_t s);
+// Authentication paths with repeats: out[((j layers + l) 8 + w)] = word w of the sibling at layer l
+// (leaves: l = 0) of the ancestor of leaf idx[j], i.e. node (2^(layers+1) - 2^(layers+1-l)) +
+// ((idx[j] >> l) ^ 1) of the node array; the host picks the reference's deduplicated node order
+// out of these q x layers digests.
+cudaError_t launch_gather_paths(const uint32_t* nodes, const uint64_t* idx, size_t q, int layers, uint32_t* out,
+                                cudaStream_t s);
 
 // ---------------------------------------------------------------------------------------------
 // Sumcheck-side kernels (reference algebra/sumcheck.rs, multilinear.rs, algebra/mod.rs)

@@ -766,10 +766,11 @@ std::vector<std::unique_ptr<whir_witness>> irs_commit_batch(whir_ctx* ctx, const
 // the two halves without changing the transcript.
 template <class F>
 struct OpenState {
-  size_t q = 0, nc = 0, nwit = 0, nodes = 0;
+  size_t q = 0, nc = 0, nwit = 0, layers = 0;
+  std::vector<uint64_t> idx;  // opened leaves in challenge order
   DBuf<uint64_t> d_idx;
   DBuf<F> d_rows;        // nwit x q x nc
-  DBuf<uint32_t> d_sib;  // nwit x nodes x 8 words
+  DBuf<uint32_t> d_sib;  // nwit x q x layers x 8 words: every query's path, repeats included
   std::vector<F> sub;
   std::vector<uint8_t> sib;
   MailFetch fetch;
@@ -793,13 +794,14 @@ void irs_open_begin(whir_ctx* ctx, const Irs& c, Transcript& ts, const std::vect
   st.nc = c.num_cols;
   st.q = idx.size();
   st.nwit = ws.size();
-  std::vector<uint64_t> nodes_idx = merkle_open_nodes(c.layers, idx);
-  st.nodes = nodes_idx.size();
-  st.d_idx = DBuf<uint64_t>(ctx, std::max<size_t>(st.q + st.nodes, 1));
-  std::vector<uint64_t> both(idx);
-  both.insert(both.end(), nodes_idx.begin(), nodes_idx.end());
-  h2d(ctx, st.d_idx.p, both.data(), both.size() * sizeof(uint64_t));
-  const size_t per_rows = st.q * st.nc, per_sib = st.nodes * 8;
+  st.layers = c.layers;
+  // The device gathers every query's whole authentication path (repeats included); the host picks
+  // the reference's deduplicated node order out of it in irs_open_end, after more device work has
+  // been queued, so that walk is off the device's critical path.
+  st.d_idx = DBuf<uint64_t>(ctx, std::max<size_t>(st.q, 1));
+  h2d(ctx, st.d_idx.p, idx.data(), idx.size() * sizeof(uint64_t));
+  st.idx = std::move(idx);
+  const size_t per_rows = st.q * st.nc, per_sib = st.q * st.layers * 8;
   st.d_rows = DBuf<F>(ctx, std::max<size_t>(st.nwit * per_rows, 1));
   st.d_sib = DBuf<uint32_t>(ctx, std::max<size_t>(st.nwit * per_sib, 1));
   for (size_t k = 0; k < ws.size(); ++k) {
@@ -809,18 +811,42 @@ void irs_open_begin(whir_ctx* ctx, const Irs& c, Transcript& ts, const std::vect
     ProfScope prof(ctx, PF_GATHER);
     CU(launch_gather_rows<F>(reinterpret_cast<const F*>(w->matrix.p), st.nc, st.d_idx.p, st.q,
                              st.d_rows.p + k * per_rows, ctx->stream));
-    CU(launch_gather_digests(w->nodes.p, st.d_idx.p + st.q, st.nodes, st.d_sib.p + k * per_sib, ctx->stream));
+    CU(launch_gather_paths(w->nodes.p, st.d_idx.p, st.q, (int)st.layers, st.d_sib.p + k * per_sib, ctx->stream));
   }
   st.sub.resize(st.nwit * per_rows);
-  st.sib.resize(st.nwit * st.nodes * 32);
+  st.sib.resize(st.nwit * per_sib * 4);
   st.fetch = mail_begin(ctx, st.sub.data(), st.d_rows.p, st.sub.size() * sizeof(F), st.sib.data(), st.d_sib.p,
                         st.sib.size());
 }
 
 template <class F>
 void irs_open_end(whir_ctx* ctx, Transcript& ts, OpenState<F>& st, std::vector<F>& rows) {
+  // Authentication nodes in the reference's order (merkle_tree.rs:145-186, as merkle_open_nodes):
+  // per layer, the siblings of the sorted distinct ancestors that are not themselves present; each
+  // ancestor keeps a query that reaches it, whose gathered path holds the sibling's digest.
+  std::vector<std::pair<uint64_t, uint32_t>> cur, next;  // (ancestor, query)
+  for (size_t j = 0; j < st.q; ++j) cur.push_back({st.idx[j], (uint32_t)j});
+  std::stable_sort(cur.begin(), cur.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
+  cur.erase(std::unique(cur.begin(), cur.end(), [](const auto& x, const auto& y) { return x.first == y.first; }),
+            cur.end());
+  std::vector<uint32_t> pick;  // (query j, layer l) of each hint node, as j * layers + l
+  for (size_t l = 0; l < st.layers; ++l) {
+    next.clear();
+    for (size_t i = 0; i < cur.size(); ++i) {
+      const uint64_t a = cur[i].first;
+      const uint32_t j = cur[i].second;
+      if (i + 1 < cur.size() && cur[i + 1].first == (a ^ 1))
+        ++i;
+      else
+        pick.push_back((uint32_t)(j * st.layers + l));
+      next.push_back({a >> 1, j});
+    }
+    cur.swap(next);
+  }
+  const size_t nodes = pick.size();
   mail_end(ctx, st.fetch);
   const size_t nc = st.nc, q = st.q, stride = st.nwit * nc, per_rows = q * nc;
+  std::vector<uint8_t> path(nodes * 32);
   rows.assign(q * stride, F::zero());
   for (size_t k = 0; k < st.nwit; ++k) {
     const F* sub = st.sub.data() + k * per_rows;
@@ -832,7 +858,9 @@ void irs_open_end(whir_ctx* ctx, Transcript& ts, OpenState<F>& st, std::vector<F
     std::vector<uint8_t> eb(per_rows * 8 * F::LIMBS);
     for (size_t i = 0; i < per_rows; ++i) elem_bytes(sub[i], eb.data() + i * 8 * F::LIMBS);
     ts.hint_bytes(eb.data(), eb.size());
-    ts.hint_bytes(st.sib.data() + k * st.nodes * 32, st.nodes * 32);
+    const uint8_t* all = st.sib.data() + k * q * st.layers * 32;
+    for (size_t n = 0; n < nodes; ++n) memcpy(path.data() + n * 32, all + (size_t)pick[n] * 32, 32);
+    ts.hint_bytes(path.data(), path.size());
     for (size_t pi = 0; pi < q; ++pi)
       for (size_t j = 0; j < nc; ++j) rows[pi * stride + k * nc + j] = sub[pi * nc + j];
   }
