@@ -567,18 +567,6 @@ cudaError_t launch_pow(const uint32_t challenge[8], uint64_t threshold, uint64_t
 
 // ---------------------------------------------------------------------------------------------
 
-__global__ void gather_digests_kernel(const uint32_t* nodes, const uint64_t* idx, uint64_t n, uint32_t* out) {
-  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n * 8; t += (uint64_t)gridDim.x * blockDim.x)
-    out[t] = nodes[idx[t >> 3] * 8 + (t & 7)];
-}
-cudaError_t launch_gather_digests(const uint32_t* nodes, const uint64_t* idx, size_t n, uint32_t* out, cudaStream_t s) {
-  if (n == 0) return cudaSuccess;
-  unsigned grid = (unsigned)std::min<size_t>((n * 8 + 255) / 256, 4096);
-  gather_digests_kernel<<<grid, 256, 0, s>>>(nodes, idx, n, out);
-  note_launch();
-  return cudaGetLastError();
-}
-
 __global__ void gather_paths_kernel(const uint32_t* nodes, const uint64_t* idx, uint64_t q, int layers, uint32_t* out) {
   const uint64_t total = q * (uint64_t)layers * 8;
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total; t += (uint64_t)gridDim.x * blockDim.x) {

@@ -179,8 +179,6 @@ cudaError_t launch_pow(const uint32_t challenge[8], uint64_t threshold, uint64_t
 // out[i*cols .. (i+1)*cols) = matrix[idx[i]*cols ..]
 template <class F>
 cudaError_t launch_gather_rows(const F* matrix, size_t cols, const uint64_t* idx, size_t n, F* out, cudaStream_t s);
-cudaError_t launch_gather_digests(const uint32_t* nodes, const uint64_t* idx, size_t n, uint32_t* out,
-                                  cudaStream_t s);
 // Authentication paths with repeats: out[((j layers + l) 8 + w)] = word w of the sibling at layer l
 // (leaves: l = 0) of the ancestor of leaf idx[j], i.e. node (2^(layers+1) - 2^(layers+1-l)) +
 // ((idx[j] >> l) ^ 1) of the node array; the host picks the reference's deduplicated node order
@@ -306,7 +304,7 @@ cudaError_t launch_eq_table(const T* point, int off, int cnt, T scalar, T* table
 // vectors gives the 2^k sums from which the host derives all k round messages (launch_tensor_sums),
 // a second pass after the last challenge writes the folded a and b (launch_tensor_fold). The
 // tables hold, per form, the tensor weights of variables k..n-1 split into rows then columns
-// (built by launch_tensor_table from per-variable (alpha, beta) pairs).
+// (built by launch_tensor_tables from per-variable (alpha, beta) pairs).
 static constexpr int TS_THREADS = 256;
 static constexpr int TS_MAX_FORMS = 4;
 static constexpr int TS_MAX_RPC = 32;  // rows per CTA in the sums pass
@@ -350,11 +348,9 @@ cudaError_t launch_tensor_sums(const S* x, const TensorShape& sh, const T* table
 template <class T, class S>
 cudaError_t launch_tensor_fold(const S* x, const TensorShape& sh, const T* w, const T* kf, const T* tables, T* a_out,
                                T* b_out, unsigned int* err, cudaStream_t s);
-// out[e] = scalar * prod_q (bit_{cnt-1-q}(e) ? ab[2q+1] : ab[2q]) for e < 2^cnt (device arrays).
-template <class T>
-cudaError_t launch_tensor_table(const T* ab, int cnt, T scalar, T* out, cudaStream_t s);
 // Every form's row table (2^R) and column table (2^C) in one launch, from 2 (R + C) (alpha, beta)
-// values per form; out holds nforms x (2^R + 2^C) entries, form-major, rows first.
+// values per form; out holds nforms x (2^R + 2^C) entries, form-major, rows first, entry e of a
+// table over cnt variables being prod_q (bit_{cnt-1-q}(e) ? beta_q : alpha_q).
 template <class T>
 cudaError_t launch_tensor_tables(const T* ab, int nforms, int R, int C, T* out, cudaStream_t s);
 

@@ -718,31 +718,4 @@ inline std::vector<uint8_t> config_bytes(const Config& c) {
   return w.out;
 }
 
-// Sibling digests a Merkle opening must reveal, in the order merkle_tree.rs:145-186 writes them;
-// returned as absolute node indices into the [leaves][layer 1]...[root] layout.
-inline std::vector<uint64_t> merkle_open_nodes(size_t layers, std::vector<uint64_t> idx) {
-  std::sort(idx.begin(), idx.end());
-  idx.erase(std::unique(idx.begin(), idx.end()), idx.end());
-  std::vector<uint64_t> out, next;
-  out.reserve(idx.size() * layers);
-  next.reserve(idx.size());
-  uint64_t off = 0, len = 1ull << layers;
-  while (len > 1) {
-    next.clear();
-    for (size_t i = 0; i < idx.size(); ++i) {
-      uint64_t a = idx[i];
-      if (i + 1 < idx.size() && idx[i + 1] == (a ^ 1)) {
-        ++i;
-      } else {
-        out.push_back(off + (a ^ 1));
-      }
-      next.push_back(a >> 1);
-    }
-    idx.swap(next);
-    off += len;
-    len >>= 1;
-  }
-  return out;
-}
-
 }  // namespace whir

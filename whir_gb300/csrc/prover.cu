@@ -821,7 +821,7 @@ void irs_open_begin(whir_ctx* ctx, const Irs& c, Transcript& ts, const std::vect
 
 template <class F>
 void irs_open_end(whir_ctx* ctx, Transcript& ts, OpenState<F>& st, std::vector<F>& rows) {
-  // Authentication nodes in the reference's order (merkle_tree.rs:145-186, as merkle_open_nodes):
+  // Authentication nodes in the reference's order (merkle_tree.rs:145-186):
   // per layer, the siblings of the sorted distinct ancestors that are not themselves present; each
   // ancestor keeps a query that reaches it, whose gathered path holds the sibling's digest.
   std::vector<std::pair<uint64_t, uint32_t>> cur, next;  // (ancestor, query)

@@ -1516,17 +1516,6 @@ __global__ void __launch_bounds__(TS_THREADS, sizeof(T) <= 8 ? 4 : (sizeof(T) <=
   b_out[i + 1] = b1;
 }
 
-// Tensor table of `cnt` variables: out[e] = scalar * prod_q (bit_{cnt-1-q}(e) ? ab[2q+1] : ab[2q]).
-template <class T>
-__global__ void tensor_table_kernel(const T* ab, int cnt, T scalar, T* out) {
-  const uint64_t size = 1ull << cnt;
-  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < size; e += (uint64_t)gridDim.x * blockDim.x) {
-    T v = scalar;
-    for (int q = 0; q < cnt; ++q) v = v * ab[2 * q + ((e >> (cnt - 1 - q)) & 1)];
-    out[e] = v;
-  }
-}
-
 template <class T, class S, int NF>
 static cudaError_t run_tensor_sums_bulk(const S* x, const TensorShape& sh, const T* tables, T* partials, T* out,
                                         unsigned int* counter, cudaStream_t s, const MailSlot& mail) {
@@ -1647,13 +1636,6 @@ cudaError_t launch_tensor_tables(const T* ab, int nforms, int R, int C, T* out, 
   return cudaGetLastError();
 }
 
-template <class T>
-cudaError_t launch_tensor_table(const T* ab, int cnt, T scalar, T* out, cudaStream_t s) {
-  tensor_table_kernel<T><<<(unsigned)std::max<size_t>(1, ((1ull << cnt) + 255) / 256), 256, 0, s>>>(ab, cnt, scalar,
-                                                                                                   out);
-  note_launch();
-  return cudaGetLastError();
-}
 
 // ---------------------------------------------------------------------------------------------
 // Multilinear evaluation sum_i map(x_i) * eq(point, i) with the eq weights taken from one pair of
@@ -1752,7 +1734,6 @@ cudaError_t launch_univariate_eval(const S* coeffs, size_t n, T x, T* partials, 
   template cudaError_t launch_add<T>(T*, const T*, size_t, cudaStream_t);                                        \
   template cudaError_t launch_eq_table<T>(const T*, int, int, T, T*, cudaStream_t);                              \
   template cudaError_t launch_rows_finish<T>(T*, size_t, T, const T*, int, const T*, int, int, T*, cudaStream_t);  \
-  template cudaError_t launch_tensor_table<T>(const T*, int, T, T*, cudaStream_t);                                \
   template cudaError_t launch_tensor_tables<T>(const T*, int, int, int, T*, cudaStream_t);
 
 // Kernels that read coefficient vectors over S and compute over T.
