@@ -232,8 +232,8 @@ int whir_pow_grind(whir_ctx* ctx, const uint8_t engine_id[32], const uint8_t cha
 
 /* ---- no-allocation variant ---------------------------------------------------------------------
  * No counterpart in the reference. eval_eq (acc += scalar * eq(point, .)) for callers that cannot
- * call cudaMalloc where they need it: code inside a CUDA stream capture, hosts that embed the
- * prover behind an allocator they do not control, callers with a fixed device-memory budget. It
+ * call cudaMalloc where they need it: hosts that embed the prover behind an allocator they do not
+ * control, callers with a fixed device-memory budget or that must not allocate at the call site. It
  * needs no whir_ctx and allocates nothing: acc_dev (2^nvars elements) and point_dev (nvars
  * elements) are caller-owned device buffers on the current device, scalar is one host element,
  * stream is a cudaStream_t (NULL = legacy default stream); the work is only enqueued.
@@ -243,10 +243,9 @@ int whir_pow_grind(whir_ctx* ctx, const uint8_t engine_id[32], const uint8_t cha
  *     (2^ceil(nvars/2) + 2^floor(nvars/2)) * element bytes <= 256 KiB: nvars <= 28 for Goldilocks1,
  *     <= 26 for Goldilocks2, <= 24 for Goldilocks3. Larger nvars (or nvars == 0) is rejected with
  *     WHIR_ERR_INVALID.
- *   - Each call made outside a stream capture looks up the array's device address on the current
- *     device (cudaGetSymbolAddress); a call made while `stream` is capturing reuses the address of
- *     the last such call on that device, so make one call on each device before any capture (and
- *     again after a device reset).
+ *   - Each call looks up the array's device address on the current device (cudaGetSymbolAddress),
+ *     except while `stream` reports an active capture (cudaStreamIsCapturing), when it reuses the
+ *     address found by the last call on that device that did look it up.
  *   - All calls share the array and it keeps the last call's tables; every call rewrites the
  *     tables before reading them. Calls whose work overlaps on the GPU (different streams, or
  *     different host threads on the same device) race on the array: serialise them.

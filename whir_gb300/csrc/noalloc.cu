@@ -1,15 +1,14 @@
 // eval_eq for callers that cannot allocate device memory.
 //
-// Some callers cannot call cudaMalloc at the point where they need this operation: code running
-// inside a CUDA stream capture (allocation is not a capturable operation), host libraries that
-// embed the prover behind an allocator they do not control, or callers holding a fixed memory
-// budget. whir_eval_eq_noalloc takes only caller-owned device buffers and keeps its one piece of
+// Some callers cannot call cudaMalloc at the point where they need this operation: host libraries
+// that embed the prover behind an allocator they do not control, callers holding a fixed memory
+// budget, or code that must not allocate at the call site. whir_eval_eq_noalloc takes only caller-owned device buffers and keeps its one piece of
 // scratch (the two eq tables) in a file-scope device array, so it performs no allocation at all.
 //
 // The scratch array lives for as long as the library is loaded, on every device that loads it.
 // Host code cannot use the array's name as a device address (in host code the symbol is only a
 // host-side stand-in), so the device address is looked up with cudaGetSymbolAddress, with the
-// device current, by each call made outside a stream capture.
+// device current (see scratch_address for when a call reuses an earlier lookup).
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -35,10 +34,10 @@ int fail(int code, const std::string& m) {
   return code;
 }
 
-// Device address of the scratch array on the current device. Looked up again on every call made
-// outside a stream capture (the lookup is cheap, and a fresh one stays valid after a device reset or
-// in a context other than the one of an earlier call); a call made while `stream` is capturing uses
-// the address found by the last call on this device that was not capturing.
+// Device address of the scratch array on the current device. Looked up again on every call (the
+// lookup is cheap, and a fresh one stays valid after a device reset or in a context other than the
+// one of an earlier call), except while `stream` reports an active capture, when the address found
+// by the last looking-up call on this device is reused.
 int scratch_address(int device, cudaStream_t stream, void** out) {
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   const cudaError_t qe = cudaStreamIsCapturing(stream, &cs);
