@@ -95,11 +95,13 @@ def test_served_proofs_identical_to_alone(ctx):
         assert j.narg == narg and j.hints == hints, j.session
 
 
-def test_served_proofs_identical_with_priority_workers(ctx):
-    # Small requests on raised-priority contexts, large ones elsewhere: proofs are unchanged.
+@pytest.mark.parametrize("policy", [dict(priority_workers=1), dict(priority_workers=1, priority_large=True),
+                                    dict(max_work=3 << 12)])
+def test_served_proofs_identical_with_other_policies(ctx, policy):
+    # One size class on raised-priority contexts, or a cap on the work in service: proofs are unchanged.
     jobs = _small_jobs(ctx, 10, seed=14)
     ref = _alone(ctx, jobs)
-    srv = serving.ProofServer(device=0, workers=3, hbm_budget=1 << 40, priority_workers=1, large_nv=12)
+    srv = serving.ProofServer(device=0, workers=3, hbm_budget=1 << 40, large_nv=12, **policy)
     try:
         srv.run(jobs, serving.poisson_arrivals(len(jobs), 800.0, seed=4))
     finally:

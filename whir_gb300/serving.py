@@ -197,19 +197,27 @@ class ProofServer:
     """Continuous batching over `workers` contexts with admission by an HBM budget (bytes).
 
     With priority_workers > 0, that many of the workers own contexts with raised stream priority and
-    take the oldest admitted request of fewer than 2^large_nv coefficients first; the other workers
-    take the oldest larger request first. Either falls back to the oldest request of any size. The
-    kernels of small requests then go ahead of the pending blocks of large ones, so a small request's
-    service time stays near its time alone while the large requests absorb the wait."""
+    take the oldest admitted request of fewer than 2^large_nv coefficients first (priority_large:
+    of at least 2^large_nv); the other workers take the oldest request of the other class first.
+    Either falls back to the oldest request of any size. The kernels of the favoured class then go
+    ahead of the pending blocks of the other's.
 
-    def __init__(self, device=0, workers=8, hbm_budget=150 << 30, priority_workers=0, large_nv=22):
+    With max_work set, a request starts only while the coefficients (batch_size x 2^nv) of the
+    requests in service plus its own stay within max_work, or when none is in service; requests
+    start strictly oldest first. Fewer large requests then share the device at once, so each runs
+    closer to its time alone, at the cost of more queueing."""
+
+    def __init__(self, device=0, workers=8, hbm_budget=150 << 30, priority_workers=0, large_nv=22,
+                 priority_large=False, max_work=None):
         priority_workers = max(0, min(priority_workers, workers))
         self.contexts = [Context(device, priority=1) for _ in range(priority_workers)]
         self.contexts += [Context(device) for _ in range(workers - priority_workers)]
-        self.prefers_large = [False] * priority_workers + [True] * (workers - priority_workers)
+        favoured = bool(priority_large)
+        self.prefers_large = [favoured] * priority_workers + [not favoured] * (workers - priority_workers)
         self.large_nv = large_nv
         self.split = priority_workers > 0
         self.budget = hbm_budget
+        self.max_work = max_work
 
     def run(self, jobs, arrivals):
         """Replays a request trace: job i arrives `arrivals[i]` seconds after the start. Returns
@@ -220,10 +228,11 @@ class ProofServer:
         est = [j.memory_estimate() for j in jobs]
         if any(e > self.budget for e in est):
             raise ValueError("a request exceeds the HBM budget on its own")
+        work = [j.vectors.shape[0] << j.nv for j in jobs]
         cv = threading.Condition()
         pending = collections.deque()  # arrived, not yet admitted (FIFO)
         admitted = collections.deque()  # admitted, waiting for a worker
-        state = {"in_use": 0, "taken": 0, "error": None}
+        state = {"in_use": 0, "taken": 0, "work": 0, "error": None}
         t0 = time.perf_counter()
 
         def admit_locked():
@@ -243,24 +252,34 @@ class ProofServer:
                     admit_locked()
                     cv.notify_all()
 
-        def take_locked(large):
-            # oldest admitted request of the preferred size class, else the oldest of any
+        def pick_locked(large):
+            # position of the oldest admitted request of the preferred size class, else of the oldest
+            # of any; None while the work cap holds it back
+            k = 0
             if self.split:
-                for k, i in enumerate(admitted):
-                    if (jobs[i].nv >= self.large_nv) == large:
-                        del admitted[k]
-                        return i
-            return admitted.popleft()
+                k = next((q for q, i in enumerate(admitted) if (jobs[i].nv >= self.large_nv) == large), 0)
+            i = admitted[k]
+            if self.max_work is not None and state["work"] > 0 and state["work"] + work[i] > self.max_work:
+                return None
+            return k
 
         def worker(ctx, large):
             while True:
                 with cv:
-                    while not admitted and state["taken"] < n and state["error"] is None:
+                    while True:
+                        if state["error"] is not None:
+                            return  # failed elsewhere
+                        if admitted:
+                            k = pick_locked(large)
+                            if k is not None:
+                                break
+                        elif state["taken"] >= n:
+                            return  # every job has been taken
                         cv.wait(timeout=0.05)
-                    if state["error"] is not None or not admitted:
-                        return  # failed elsewhere, or every job has been taken
-                    i = take_locked(large)
+                    i = admitted[k]
+                    del admitted[k]
                     state["taken"] += 1
+                    state["work"] += work[i]
                     jobs[i].start = time.perf_counter()
                 try:
                     prove_job(ctx, jobs[i])
@@ -272,6 +291,7 @@ class ProofServer:
                 with cv:
                     jobs[i].done = time.perf_counter()
                     state["in_use"] -= est[i]
+                    state["work"] -= work[i]
                     admit_locked()
                     cv.notify_all()
 
