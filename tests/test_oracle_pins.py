@@ -10,6 +10,8 @@ import pytest
 
 from whir_gb300.inputs import GOLDILOCKS_P as P, Rng, field_elements
 
+import blake3_spec
+
 KATS = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_kats.json")))
 
 
@@ -28,6 +30,18 @@ def test_engine_ids_match_reference_and_hashlib(orc):
 def test_blake3_empty_hash(orc):
     # blake3_engine.rs:23 EMPTY_HASH pins the compression function, IV and flags
     assert orc.hash_many(orc.ENGINE_BLAKE3, 0, b"", 3) == bytes.fromhex(KATS["blake3_empty_hash"]["hex"]) * 3
+
+
+@pytest.mark.parametrize("n", [1, 63, 64, 65, 128, 200, 576, 1023, 1024, 1025, 2048, 2049, 3072, 4096, 4097, 9000])
+def test_blake3_against_spec_restatement(orc, n):
+    # Several blocks per chunk, partial last blocks and the parent-node tree above one chunk, checked
+    # against a plain-Python restatement of the BLAKE3 specification, itself pinned by EMPTY_HASH.
+    assert blake3_spec.blake3(b"") == bytes.fromhex(KATS["blake3_empty_hash"]["hex"])
+    rng = np.random.default_rng(1000 + n)
+    for count in (1, 2):
+        msgs = rng.integers(0, 256, size=n * count, dtype=np.uint8).tobytes()
+        exp = b"".join(blake3_spec.blake3(msgs[i * n:(i + 1) * n]) for i in range(count))
+        assert orc.hash_many(orc.ENGINE_BLAKE3, n, msgs, count) == exp
 
 
 @pytest.mark.parametrize("n", [0, 1, 3, 31, 32, 64, 100, 135, 136, 137, 271, 272, 500, 1024])
