@@ -203,9 +203,10 @@ class ProofServer:
     ahead of the pending blocks of the other's.
 
     With max_work set, a request starts only while the coefficients (batch_size x 2^nv) of the
-    requests in service plus its own stay within max_work, or when none is in service; requests
-    start strictly oldest first. Fewer large requests then share the device at once, so each runs
-    closer to its time alone, at the cost of more queueing."""
+    requests in service plus its own stay within max_work, or when none is in service; a worker
+    whose pick (the oldest request, or with priority workers the oldest of its class) does not fit
+    waits rather than taking a later one. Fewer large requests then share the device at once, so
+    each runs closer to its time alone, at the cost of more queueing."""
 
     def __init__(self, device=0, workers=8, hbm_budget=150 << 30, priority_workers=0, large_nv=22,
                  priority_large=False, max_work=None):
