@@ -38,7 +38,8 @@ class FakeJob:
 class Recorder:
     """prove_job stand-in: sleeps in proportion to the request's size and records what was in service."""
 
-    def __init__(self):
+    def __init__(self, scale=0.0005):
+        self.scale = scale  # seconds of sleep for a 2^10-coefficient request
         self.lock = threading.Lock()
         self.running = []
         self.max_work_seen = []
@@ -51,7 +52,7 @@ class Recorder:
             self.max_work_seen.append((len(self.running), work))
             self.max_mem_seen = max(self.max_mem_seen, sum(j.mem for j in self.running))
         job.ctx = ctx
-        time.sleep(0.0005 * (1 << (job.nv - 10)))
+        time.sleep(self.scale * (1 << (job.nv - 10)))
         with self.lock:
             self.running.remove(job)
         return job
@@ -120,7 +121,9 @@ def test_request_over_cap_runs_alone(fake):
 @pytest.mark.parametrize("large", [False, True])
 def test_priority_workers_take_their_class_first(fake, large):
     # Two long requests hold both workers while two small and two large ones queue up; the priority
-    # worker's next request is then the oldest of its class.
+    # worker's next request is then the oldest of its class. Slow stand-in proofs (the large ones take
+    # 32 ms) keep the outcome clear of thread-scheduling jitter.
+    fake.scale = 0.002
     jobs = [FakeJob(16), FakeJob(16), FakeJob(10), FakeJob(14), FakeJob(10), FakeJob(14)]
     srv = serving.ProofServer(workers=2, hbm_budget=1 << 40, priority_workers=1, large_nv=12,
                               priority_large=large)
